@@ -1,0 +1,323 @@
+"""Benchmark of the forward model on the crossing-bundle workload.
+
+One step = the forward model of one volume: voxelize 2 x 1000 fibers of 50
+points into a 512x512x120 volume at 0.2 µm (generate_tissue) and march it at
+5 tilts ((0,0) and 5.5° at phi = 0/90/180/270°) x 9 polarizer angles with
+Slerp interpolation (run_simulation), epa fused.  Synthetic seeded fibers
+(``fastpli_gb300.synth.crossing``); the label + vector volume (503 MB) is
+larger than L2, so no flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line (rank 0).  ``value`` is ray-voxel steps per second of
+the whole step, device-resident; ``e2e`` the same metric through the
+drop-in host API (host numpy in and out, copies inside the timed region).
+``--impl reference`` times the CPU forward model (the oracle's C
+restatement of the reference, all host threads) on the same workload.
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ray-voxel steps/s (forward model: voxelize + 5 tilts x 9 angles, Slerp)"
+UNIT = "steps/s"
+
+
+def _dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _workload(rank=0):
+    from fastpli_gb300 import synth
+    # every rank voxelizes and marches its own seeded volume (weak scaling)
+    return synth.crossing(seed=2 + rank)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                      "--format=csv,noheader,nounits"],
+                                     capture_output=True, text=True, timeout=5).stdout.strip()
+                if out:
+                    self.rows.append([c.strip() for c in out.split(",")])
+            except Exception:
+                return
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in self.rows for n, v in zip(names, r[3:7]) if v == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _setup_args(w):
+    kw = w.setup_kwargs()
+    return (kw["step_size"], kw["light_intensity"], kw["voxel_size"], kw["wavelength"],
+            kw["tissue_refrection"], kw["interpolate"], kw["untilt_sensor_view"],
+            kw["flip_z"], kw["filter_rotations"])
+
+
+# ---------------------------------------------------------------- CPU arm ---
+def cpu_forward(w, n_threads, tilts=None):
+    """The oracle's C restatement of the reference forward model; returns
+    (seconds, ray-voxel steps)."""
+    import oracle
+    oracle.build(ref=False)
+    from fastpli_gb300 import _native as N
+    tilts = w.tilts if tilts is None else tilts
+    t0 = time.perf_counter()
+    lab, vec, props, _ = oracle.generate(w.dim, w.origin, w.voxel_size, w.bundles, w.layers,
+                                         n_threads=n_threads)
+    for theta, phi in tilts:
+        oracle.simulate(lab, vec, props, theta, phi, n_threads=n_threads, **w.setup_kwargs())
+    dt = time.perf_counter() - t0
+    s = N.SetupBlock(*_setup_args(w))
+    d = np.asarray(w.dim, np.int64)
+    steps = sum(int(N.load(build_if_missing=False).fpgb_count_steps(
+        N.byref(s.struct), N.ptr(d), float(t), float(p))) for t, p in tilts)
+    return dt, steps
+
+
+def run_reference(args):
+    ws, rank, _ = _dist_env()
+    if rank != 0:
+        return 0
+    w = _workload(0)
+    from fastpli_gb300 import build as nb
+    nb.build()
+    threads = os.cpu_count() or 1
+    for _ in range(max(0, min(args.warmup, 1))):
+        cpu_forward(w, threads, tilts=w.tilts[:1])
+    times, steps = [], 0
+    for _ in range(args.steps):
+        dt, steps = cpu_forward(w, threads)
+        times.append(dt)
+    value = steps / (sum(times) / len(times))
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": dict(w.describe(), inputs="fibers (host)",
+                           parallelism=f"OpenMP {threads} threads"),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": "full forward-model steps of the workload"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------- GPU arm ---
+def run_gpu(args):
+    import torch
+    ws, rank, local = _dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from fastpli_gb300.simulation import _Generator, _Simulator
+    import fastpli_gb300
+    fastpli_gb300.native_library()
+
+    w = _workload(rank)
+    X, Y, Z = (int(v) for v in w.dim)
+    g = _Generator()
+    g.set_volume(w.dim, w.origin, w.voxel_size)
+    g.set_fiber_bundles(w.bundles, w.layers)
+    sim = _Simulator()
+    sim.set_pli_setup(*_setup_args(w))
+    steps_per = sum(sim.count_steps(w.dim, float(t), float(p)) for t, p in w.tilts)
+    n_rho = sim.n_rho
+    dev = torch.device("cuda", local)
+    label = torch.empty((X, Y, Z), dtype=torch.int32, device=dev)
+    vector = torch.empty((X, Y, Z, 3), dtype=torch.float32, device=dev)
+    images = [torch.empty((X, Y, n_rho), dtype=torch.float64, device=dev) for _ in w.tilts]
+    wsp = torch.empty(g.workspace_size(), dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+    _, _, props, _ = g.run_generation_device(label=label, vector=vector, workspace=wsp)
+    tissue_voxels = int((label > 0).sum().item())
+
+    def step(ev=None):
+        if ev:
+            ev[0].record(stream)
+        g.run_generation_device(label=label, vector=vector, workspace=wsp,
+                                sync_warnings=False)
+        if ev:
+            ev[1].record(stream)
+        for k, (t, p) in enumerate(w.tilts):
+            sim.run_simulation_device(w.dim, label, vector, props, float(t), float(p),
+                                      image=images[k], sync_warnings=False)
+        if ev:
+            ev[2].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for i in range(args.steps):
+            step(evs[i])
+        t1.record(stream)
+        torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ms_total = t0.elapsed_time(t1)
+    gen_ms = [e[0].elapsed_time(e[1]) for e in evs]
+    march_ms = [e[1].elapsed_time(e[2]) for e in evs]
+    if dist:
+        tt = torch.tensor([ms_total], device=dev, dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms_total = float(tt.item())
+    ms_step = ms_total / args.steps
+    value = ws * steps_per / (ms_step * 1e-3)
+
+    # ----- e2e through the drop-in host API (numpy in/out) ---------------
+    e2e_steps = max(1, min(args.steps, 3))
+    lab_h, vec_h, props_h = g.run_generation()
+    sim.run_simulation(w.dim, lab_h, vec_h, props_h, 0.0, 0.0)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    t_e2e = time.perf_counter()
+    for _ in range(e2e_steps):
+        lab_h, vec_h, props_h = g.run_generation()
+        imgs = [sim.run_simulation(w.dim, lab_h, vec_h, props_h, float(t), float(p))
+                for t, p in w.tilts]
+    e2e_s = (time.perf_counter() - t_e2e) / e2e_steps
+    if dist:
+        tt = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    vol_bytes = X * Y * Z * 16
+    img_bytes = X * Y * n_rho * 8
+    fib_bytes = int(sum(f.nbytes for b in w.bundles for f in b))
+    h2d = fib_bytes + len(w.tilts) * vol_bytes
+    d2h = vol_bytes + len(w.tilts) * img_bytes
+    del imgs
+
+    # ----- roofline of the dominant kernel ------------------------------
+    hbm_peak, peak_kind = _peaks()
+    gen_avg = sum(gen_ms) / len(gen_ms)
+    march_avg = sum(march_ms) / len(march_ms)
+    march_bytes = 16 * steps_per
+    march_gbs = march_bytes / (march_avg * 1e-3) / 1e9
+    # voxelizer algorithmic bytes: key init + key read (8+8) and label/vector
+    # write (16) per voxel
+    gen_bytes = 32 * X * Y * Z
+    gen_gbs = gen_bytes / (gen_avg * 1e-3) / 1e9
+    if march_avg >= gen_avg:
+        roof = {"kernel": "march_rays (5 tilts)", "bound": "hbm", "achieved": march_gbs,
+                "peak": hbm_peak, "unit": "GB/s", "frac": march_gbs / hbm_peak,
+                "traffic": None, "algorithmic_bytes_per_step": 16, "peak_source": peak_kind}
+    else:
+        roof = {"kernel": "tissue_keys+tissue_write", "bound": "hbm", "achieved": gen_gbs,
+                "peak": hbm_peak, "unit": "GB/s", "frac": gen_gbs / hbm_peak,
+                "traffic": None, "algorithmic_bytes_per_voxel": 32, "peak_source": peak_kind}
+
+    line = None
+    if rank == 0:
+        cpu = None
+        if ws == 1 and not args.no_cpu:
+            threads = os.cpu_count() or 1
+            dt, st = cpu_forward(w, threads)
+            cpu = {"value": st / dt, "unit": UNIT, "cores": threads, "kind": "port",
+                   "sample": "one full forward-model step of the workload (oracle C "
+                             "restatement, OpenMP)"}
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": dict(w.describe(), l2="inputs larger than L2 (503 MB volume)",
+                           parallelism=f"replicas x{ws}"),
+            "tissue_voxels_per_s": tissue_voxels / (gen_avg * 1e-3),
+            "voxelize_ms": gen_avg, "march_ms": march_avg,
+            "march_steps_per_s": steps_per / (march_avg * 1e-3),
+            "roofline": roof, "cpu_baseline": cpu,
+            "e2e": {"value": ws * steps_per / e2e_s, "unit": UNIT,
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": args.steps * (2 + len(w.tilts)),
+            "clocks": clocks.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

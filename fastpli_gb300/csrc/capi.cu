@@ -1,0 +1,115 @@
+// Library-wide C-ABI helpers: error string, version, cached device pool.
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <utility>
+
+#include "fpgb_common.cuh"
+
+namespace fpgb {
+
+static thread_local std::string g_last_error;
+
+void set_error(const char *fmt, ...) {
+   char buf[1024];
+   va_list ap;
+   va_start(ap, fmt);
+   vsnprintf(buf, sizeof buf, fmt, ap);
+   va_end(ap);
+   g_last_error = buf;
+}
+
+namespace {
+struct PoolEntry {
+   void *ptr = nullptr;
+   size_t bytes = 0;
+};
+std::mutex g_pool_mu;
+struct PoolKey {
+   int dev;
+   uintptr_t stream;
+   int slot;
+   bool operator<(const PoolKey &o) const {
+      if (dev != o.dev)
+         return dev < o.dev;
+      if (stream != o.stream)
+         return stream < o.stream;
+      return slot < o.slot;
+   }
+};
+std::map<PoolKey, PoolEntry> g_pool;
+} // namespace
+
+int pool_get(int slot, size_t bytes, void **ptr, cudaStream_t stream) {
+   int dev = 0;
+   FPGB_CUDA_TRY(cudaGetDevice(&dev));
+   std::lock_guard<std::mutex> lk(g_pool_mu);
+   PoolEntry &e = g_pool[PoolKey{dev, reinterpret_cast<uintptr_t>(stream), slot}];
+   if (e.bytes < bytes) {
+      if (e.ptr) {
+         // Buffers of this slot may still be in use by work queued on any
+         // stream: wait for the device before giving the memory back.
+         FPGB_CUDA_TRY(cudaDeviceSynchronize());
+         FPGB_CUDA_TRY(cudaFree(e.ptr));
+         e.ptr = nullptr;
+         e.bytes = 0;
+      }
+      size_t want = align_up(bytes < 256 ? 256 : bytes, 1 << 20);
+      cudaError_t err = cudaMalloc(&e.ptr, want);
+      if (err != cudaSuccess) {
+         e.ptr = nullptr;
+         set_error("device pool: cudaMalloc(%zu) failed: %s", want,
+                   cudaGetErrorString(err));
+         return FPGB_ENOMEM;
+      }
+      e.bytes = want;
+   }
+   *ptr = e.ptr;
+   return FPGB_OK;
+}
+
+int pool_release_all() {
+   int dev = 0;
+   FPGB_CUDA_TRY(cudaGetDevice(&dev));
+   std::lock_guard<std::mutex> lk(g_pool_mu);
+   FPGB_CUDA_TRY(cudaDeviceSynchronize());
+   for (auto it = g_pool.begin(); it != g_pool.end();) {
+      if (it->first.dev == dev) {
+         if (it->second.ptr)
+            FPGB_CUDA_TRY(cudaFree(it->second.ptr));
+         it = g_pool.erase(it);
+      } else {
+         ++it;
+      }
+   }
+   return FPGB_OK;
+}
+
+int warnings_from_counters(const long long *h, fpgb_warnings *w) {
+   if (!w)
+      return FPGB_OK;
+   w->overlap = h[0];
+   w->single_point = h[1];
+   w->zero_axis = h[2];
+   w->not_normalized = h[3];
+   w->empty_light = h[4];
+   w->layer_overflow = h[5];
+   return FPGB_OK;
+}
+
+} // namespace fpgb
+
+extern "C" {
+
+const char *fpgb_last_error(void) { return fpgb::g_last_error.c_str(); }
+
+const char *fpgb_version(void) { return "fastpli_gb300 0.1.0 (sm_103a)"; }
+
+int fpgb_release_pool(void) { return fpgb::pool_release_all(); }
+
+} // extern "C"

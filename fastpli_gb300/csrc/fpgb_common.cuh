@@ -1,0 +1,76 @@
+// Shared host/device plumbing of libfastpli_gb300: error reporting, the
+// cached device pool, launch helpers.  No simulation logic lives here.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include "../../include/fastpli_gb300.h"
+
+namespace fpgb {
+
+// ---------------------------------------------------------------- errors ---
+void set_error(const char *fmt, ...);
+
+#define FPGB_CUDA_TRY(expr)                                                    \
+   do {                                                                        \
+      cudaError_t e_ = (expr);                                                 \
+      if (e_ != cudaSuccess) {                                                 \
+         ::fpgb::set_error("%s failed: %s (%s:%d)", #expr,                     \
+                           cudaGetErrorString(e_), __FILE__, __LINE__);        \
+         return FPGB_ECUDA;                                                    \
+      }                                                                        \
+   } while (0)
+
+#define FPGB_TRY(expr)                                                         \
+   do {                                                                        \
+      int rc_ = (expr);                                                        \
+      if (rc_ != FPGB_OK)                                                      \
+         return rc_;                                                           \
+   } while (0)
+
+// Device status word bits written by kernels (never __trap: a kernel that
+// detects bad input records it and carries on with a safe value).
+enum StatusBits : unsigned {
+   kStatusLabelRange = 1u << 0, // a label < 0 or >= n_props was met
+   kStatusTimeout = 1u << 1,    // a bounded wait gave up
+   kStatusOverflow = 1u << 2,   // a capacity was exceeded
+};
+
+// Per-call device counters: [0..5] fpgb_warnings order, [6] status bits,
+// [7] label min, [8] label max.
+constexpr int kCounterWords = 10;
+
+// ------------------------------------------------------------ device pool ---
+// Grow-only cache of device buffers per (device, slot), reused across calls
+// of the host-buffer entry points so repeated calls do not cudaMalloc.
+enum PoolSlot : int {
+   kSlotLabel = 0,
+   kSlotVector,
+   kSlotImage,
+   kSlotKeys,
+   kSlotSegments,
+   kSlotCounters,
+   kSlotProps,
+   kSlotEpa,
+   kSlotStaging,
+   kNumSlots
+};
+// Buffers are cached per (device, stream, slot): concurrent calls on
+// different streams never share a buffer.
+int pool_get(int slot, size_t bytes, void **ptr, cudaStream_t stream = nullptr);
+int pool_release_all();
+
+inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+inline cudaStream_t as_stream(void *s) {
+   return reinterpret_cast<cudaStream_t>(s);
+}
+
+int warnings_from_counters(const long long *h, fpgb_warnings *w);
+
+} // namespace fpgb

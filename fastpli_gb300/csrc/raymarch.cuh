@@ -1,0 +1,61 @@
+// Ray-march parameter block shared by the plain and batched kernels.
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+#include "fpgb_common.cuh"
+
+namespace fpgb {
+
+constexpr int kMaxRho = 64;
+
+// Per-label optical constants (simulator.cpp:276-288, 309-316).
+struct LabelOptics {
+   float alog; // mu[1/mm] * 1e3 * thickness : per-step -log(attenuation)
+   float kret; // pi/2 * dn * 4 * thickness / lambda : ret = kret*|v|*cos^2(alpha)
+   int32_t kind; // 0: no effect, 1: attenuation only, 2: birefringent
+   int32_t pad;
+};
+
+// One step of the z march.  Every ray of a call shares the same z sequence
+// (the start height and the z step do not depend on the pixel), so the
+// reference's double accumulation of z (simulator.cpp:259-261) is replayed on
+// the host once and tabulated.
+struct ZStep {
+   int32_t iz;  // floor(z), already mirrored when flip_z (simulator.cpp:427-428)
+   int32_t z0;  // floor(z - 0.5), not clamped, not mirrored
+   float zf;    // (z - 0.5) - z0 in [0, 1)
+   int32_t pad;
+};
+
+struct MarchParams {
+   int64_t X, Y, Z;
+   int32_t n_rho, mode, flip_z, untilt;
+   int32_t n_props, n_z, frac_bits, rotate;
+   int64_t dx_fx, dy_fx;  // x/y step in fixed point (frac_bits)
+   double hstep[3];       // light_step * 0.5
+   double hshift[2];      // 0.5 * shift (untilted view)
+   double shift[2];       // shift (tilted view)
+   double pc[3], pt[3], p1[3], p2[3];
+   double A, B, C, Dd, D; // tilted-view 2x2 system (simulator.cpp:653-668)
+   double rti[9];         // inverse tissue rotation (simulator.cpp:636-638)
+   float rot[9];          // RotZYZ(phi, theta, -phi) for the optic axis
+   double i4;             // light_intensity / 4
+   double c2r[kMaxRho], s2r[kMaxRho]; // cos 2rho, sin 2rho of the filter angles
+   double epa_sin[kMaxRho], epa_cos[kMaxRho]; // sin/cos(2*pi*i/n) of epa.py:29
+   const LabelOptics *lut;
+   const ZStep *ztab;
+};
+
+struct MarchPlan {
+   MarchParams prm;
+   std::vector<LabelOptics> lut;
+   std::vector<ZStep> ztab;
+   int64_t steps; // X*Y*n_z
+};
+
+int plan_march(const fpgb_setup *setup, const int64_t *dim, const double *props,
+               int64_t n_props, double theta, double phi, MarchPlan *plan);
+
+} // namespace fpgb

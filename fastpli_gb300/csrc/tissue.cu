@@ -1,0 +1,656 @@
+// Voxelizer: fiber polylines -> int32 label field + float32 orientation field.
+//
+// Replaces PliGenerator::RunTissueGeneration / FillVoxelsAroundFiberSegment
+// (src/simulation/generator.cpp:163-383, 475-526).  The reference walks every
+// segment in order and overwrites a voxel when `dist[ind] >= dist_squ`
+// (generator.cpp:343), so the final owner of a voxel is the segment with the
+// smallest float distance and, among equal distances, the LAST one in
+// processing order.  Here every (segment, voxel) candidate is independent:
+//
+//   pass 1  tissue_keys   one CTA per segment sweeps the segment's clipped
+//                         bounding box; a cheap FP32 test rejects voxels
+//                         clearly outside the outermost layer, survivors get
+//                         the exact double->float distance of the reference
+//                         and an atomicMin on the 64-bit key
+//                         (float bits of dist_squ) << 32 | (0xFFFFFFFF - seg),
+//                         i.e. smallest distance, then largest segment index.
+//   pass 2  tissue_write  one thread per voxel decodes the winner and
+//                         recomputes its layer and orientation exactly.
+//
+// This translation unit is compiled with -fmad=false: the label and vector
+// decisions depend on separately rounded double products and sums
+// (generator.cpp:324-349, vemath.hpp:342-344,390-402), which a fused
+// multiply-add would change.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "fpgb_common.cuh"
+#include "tissue.cuh"
+
+namespace fpgb {
+
+// ======================================================================
+// host planning (double precision, reference operation order)
+// ======================================================================
+namespace {
+
+struct Box {
+   double mn[3], mx[3];
+   void empty() {
+      for (int i = 0; i < 3; i++) {
+         mn[i] = INFINITY;
+         mx[i] = -INFINITY;
+      }
+   }
+   // aabb::AABB(p, q) unsorted constructor (aabb.hpp:54-71)
+   void from_pq(const double *p, const double *q) {
+      for (int i = 0; i < 3; i++) {
+         if (p[i] < q[i]) {
+            mn[i] = p[i];
+            mx[i] = q[i];
+         } else {
+            mn[i] = q[i];
+            mx[i] = p[i];
+         }
+      }
+   }
+   void unite(const Box &a) { // aabb.hpp:90-97
+      for (int i = 0; i < 3; i++) {
+         if (a.mn[i] < mn[i])
+            mn[i] = a.mn[i];
+         if (a.mx[i] > mx[i])
+            mx[i] = a.mx[i];
+      }
+   }
+};
+
+bool overlap(const Box &a, const Box &b) { // aabb.hpp:128-137
+   for (int i = 0; i < 3; i++)
+      if (a.mn[i] >= b.mx[i] || a.mx[i] <= b.mn[i])
+         return false;
+   return true;
+}
+
+// Fiber::CalculateVoi (fiber.cpp:83-99) of already transformed points.
+Box fiber_box(const double *xyz, const double *r, int64_t n) {
+   Box b;
+   b.empty();
+   if (n == 0)
+      return b;
+   const double lo[3] = {xyz[0] - r[0], xyz[1] - r[0], xyz[2] - r[0]};
+   const double hi[3] = {xyz[0] + r[0], xyz[1] + r[0], xyz[2] + r[0]};
+   b.from_pq(lo, hi);
+   for (int64_t s = 0; s + 1 < n; s++) {
+      const double rm = r[s] < r[s + 1] ? r[s + 1] : r[s];
+      Box t;
+      t.from_pq(xyz + 3 * s, xyz + 3 * (s + 1));
+      for (int i = 0; i < 3; i++) {
+         t.mn[i] -= rm;
+         t.mx[i] += rm;
+      }
+      b.unite(t);
+   }
+   return b;
+}
+
+} // namespace
+
+int plan_tissue(const fpgb_volume *vol, const fpgb_fibers *fb, TissuePlan *plan) {
+   if (!vol || !fb) {
+      set_error("generate_tissue: null volume or fibers");
+      return FPGB_EINVAL;
+   }
+   // SetVolume (generator.cpp:49-53,115-117)
+   if (vol->dim[0] <= 0 || vol->dim[1] <= 0 || vol->dim[2] <= 0) {
+      set_error("dim.global[any] <= 0: [%lld,%lld,%lld]",
+                (long long)vol->dim[0], (long long)vol->dim[1],
+                (long long)vol->dim[2]);
+      return FPGB_EINVAL;
+   }
+   if (!(vol->voxel_size > 0)) {
+      set_error("voxel_size <= 0: %g", vol->voxel_size);
+      return FPGB_EINVAL;
+   }
+   for (int i = 0; i < 3; i++)
+      if (vol->dim[i] > (int64_t(1) << 30)) {
+         set_error("dim[%d] = %lld exceeds 2^30", i, (long long)vol->dim[i]);
+         return FPGB_EINVAL;
+      }
+   const int64_t nb = fb->n_bundles;
+   if (nb < 0 || (nb > 0 && (!fb->bundle_fiber_off || !fb->fiber_point_off ||
+                             !fb->bundle_layer_off))) {
+      set_error("generate_tissue: malformed fiber bundle offsets");
+      return FPGB_EINVAL;
+   }
+   plan->X = vol->dim[0];
+   plan->Y = vol->dim[1];
+   plan->Z = vol->dim[2];
+   plan->n_bundles = nb;
+   plan->segs.clear();
+   plan->layers.assign(nb > 0 ? nb : 1, LayerDev{});
+   plan->single_point = 0;
+
+   // layers, sorted by scale (fiber_bundle.cpp:19-30,66,83-86)
+   int max_layer = 0;
+   for (int64_t b = 0; b < nb; b++) {
+      const int64_t l0 = fb->bundle_layer_off[b], l1 = fb->bundle_layer_off[b + 1];
+      const int n = int(l1 - l0);
+      if (n < 0 || n > kMaxLayers) {
+         set_error("bundle %lld has %d layers (1..%d supported)",
+                   (long long)b, n, kMaxLayers);
+         return FPGB_EINVAL;
+      }
+      std::vector<int> order(n);
+      for (int i = 0; i < n; i++)
+         order[i] = i;
+      std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
+         return fb->layer_scale[l0 + a] < fb->layer_scale[l0 + c];
+      });
+      LayerDev &L = plan->layers[b];
+      L.n = n;
+      for (int i = 0; i < n; i++) {
+         const int64_t l = l0 + order[i];
+         const char m = fb->layer_model[l];
+         if (m != 'b' && m != 'p' && m != 'r') {
+            set_error("Orientation must be \"b\", \"p\", or \"r\"");
+            return FPGB_EINVAL;
+         }
+         L.scale_sq[i] = fb->layer_scale[l] * fb->layer_scale[l];
+         L.model[i] = m;
+         L.dn[i] = fb->layer_dn[l];
+         L.mu[i] = fb->layer_mu[l];
+      }
+      if (n > 0) {
+         L.f_ly_squ = (float)L.scale_sq[n - 1];
+         L.sqrt_last = std::sqrt(L.scale_sq[n - 1]);
+      }
+      max_layer = std::max(max_layer, n);
+   }
+   plan->max_layer = max_layer;
+
+   // property table (generator.cpp:496-526)
+   plan->props.assign(2 * (nb * max_layer + 1), 0.0);
+   for (int64_t b = 0; b < nb; b++)
+      for (int l = 0; l < plan->layers[b].n; l++) {
+         const int64_t id = 1 + l + b * max_layer;
+         plan->props[2 * id + 1] = plan->layers[b].mu[l];
+         plan->props[2 * id] =
+             plan->layers[b].model[l] == 'b' ? 0.0 : plan->layers[b].dn[l];
+      }
+
+   // translate then resize (generator.cpp:185-197, fiber.cpp:128-150)
+   const int64_t nf = nb > 0 ? fb->bundle_fiber_off[nb] : 0;
+   const int64_t np = nf > 0 ? fb->fiber_point_off[nf] : 0;
+   if (np > 0 && !fb->points) {
+      set_error("generate_tissue: points == NULL");
+      return FPGB_EINVAL;
+   }
+   std::vector<double> xyz(3 * np), rad(np);
+   const bool translate =
+       vol->origin[0] != 0 || vol->origin[1] != 0 || vol->origin[2] != 0;
+   const double f = 1.0 / vol->voxel_size;
+   for (int64_t i = 0; i < np; i++) {
+      for (int c = 0; c < 3; c++) {
+         double v = fb->points[4 * i + c];
+         if (translate)
+            v = v + (-vol->origin[c]);
+         xyz[3 * i + c] = v * f;
+      }
+      rad[i] = fb->points[4 * i + 3] * f;
+   }
+   std::vector<Box> fbox(nf);
+   for (int64_t fi = 0; fi < nf; fi++) {
+      const int64_t p0 = fb->fiber_point_off[fi], p1 = fb->fiber_point_off[fi + 1];
+      if (p1 < p0 || p1 > np) {
+         set_error("generate_tissue: malformed fiber_point_off");
+         return FPGB_EINVAL;
+      }
+      fbox[fi] = fiber_box(xyz.data() + 3 * p0, rad.data() + p0, p1 - p0);
+   }
+   Box volbox;
+   for (int i = 0; i < 3; i++) {
+      volbox.mn[i] = 0.0;
+      volbox.mx[i] = (double)vol->dim[i];
+   }
+
+   // segment table in the reference's processing order (generator.cpp:205-231)
+   int64_t cand = 0;
+   for (int64_t b = 0; b < nb; b++) {
+      const int64_t f0 = fb->bundle_fiber_off[b], f1 = fb->bundle_fiber_off[b + 1];
+      Box bb;
+      bb.empty(); // fiber_bundle.cpp:147-154
+      if (f1 > f0)
+         bb = fbox[f0];
+      for (int64_t fi = f0; fi < f1; fi++)
+         bb.unite(fbox[fi]);
+      if (!overlap(volbox, bb))
+         continue;
+      const LayerDev &L = plan->layers[b];
+      for (int64_t fi = f0; fi < f1; fi++) {
+         const int64_t p0 = fb->fiber_point_off[fi], p1 = fb->fiber_point_off[fi + 1];
+         if (p1 - p0 <= 1) {
+            plan->single_point++;
+            continue;
+         }
+         if (!overlap(volbox, fbox[fi]))
+            continue;
+         if (L.n == 0)
+            continue;
+         for (int64_t s = p0; s + 1 < p1; s++) {
+            const double *P = &xyz[3 * s], *Q = &xyz[3 * (s + 1)];
+            const double r0 = rad[s], r1 = rad[s + 1];
+            const double rmax = (r0 < r1 ? r1 : r0) * L.sqrt_last;
+            Box sb;
+            sb.from_pq(P, Q);
+            SegDev S{};
+            int64_t count = 1;
+            for (int i = 0; i < 3; i++) {
+               sb.mn[i] -= rmax;
+               sb.mx[i] += rmax;
+               if (volbox.mn[i] > sb.mn[i])
+                  sb.mn[i] = volbox.mn[i];
+               if (volbox.mx[i] < sb.mx[i])
+                  sb.mx[i] = volbox.mx[i];
+               const int64_t lo = (int64_t)sb.mn[i];
+               const int64_t hi = (int64_t)(sb.mx[i] + 0.5);
+               S.lo[i] = (int32_t)lo;
+               S.ext[i] = (int32_t)(hi > lo ? hi - lo : 0);
+               count *= S.ext[i];
+            }
+            if (count == 0)
+               continue;
+            for (int i = 0; i < 3; i++) {
+               S.p[i] = P[i];
+               S.q[i] = Q[i];
+               S.v[i] = Q[i] - P[i];
+               const double base = std::floor(P[i]);
+               S.base[i] = (int32_t)std::max(-2147483647.0, std::min(2147483647.0, base));
+               S.pf[i] = (float)(P[i] - (double)S.base[i]);
+               S.vf[i] = (float)S.v[i];
+            }
+            {
+               double c = 0.0;
+               c = c + S.v[0] * S.v[0];
+               c = c + S.v[1] * S.v[1];
+               c = c + S.v[2] * S.v[2];
+               S.c2 = c;
+            }
+            S.c2f = (float)S.c2;
+            S.r0 = r0;
+            S.r1 = r1;
+            const double rm = r0 < r1 ? r1 : r0;
+            S.thr_f = (float)((double)L.f_ly_squ * rm * rm * (1.0 + 1e-3) + 1e-3);
+            S.bundle = (int32_t)b;
+            plan->segs.push_back(S);
+            cand += count;
+         }
+      }
+   }
+   if (plan->segs.size() > 0xFFFFFFF0ull) {
+      set_error("too many fiber segments: %zu", plan->segs.size());
+      return FPGB_EINVAL;
+   }
+   plan->candidates = cand;
+   return FPGB_OK;
+}
+
+// ======================================================================
+// device code
+// ======================================================================
+
+// Closest point of `pt` on segment S and its parameter t, in the reference's
+// double operation order (generator.cpp:475-494).  -fmad=false keeps every
+// product and sum separately rounded.
+__device__ __forceinline__ void closest_point(const SegDev &S, const double pt[3],
+                                              double cl[3], double &t) {
+   const double w0 = pt[0] - S.p[0], w1 = pt[1] - S.p[1], w2 = pt[2] - S.p[2];
+   double c1 = 0.0;
+   c1 = c1 + w0 * S.v[0];
+   c1 = c1 + w1 * S.v[1];
+   c1 = c1 + w2 * S.v[2];
+   if (c1 < 0) {
+      cl[0] = S.p[0];
+      cl[1] = S.p[1];
+      cl[2] = S.p[2];
+      t = 0.0;
+   } else if (S.c2 <= c1) {
+      cl[0] = S.q[0];
+      cl[1] = S.q[1];
+      cl[2] = S.q[2];
+      t = 1.0;
+   } else {
+      const double b = c1 / S.c2;
+      cl[0] = S.p[0] + S.v[0] * b;
+      cl[1] = S.p[1] + S.v[1] * b;
+      cl[2] = S.p[2] + S.v[2] * b;
+      t = b;
+   }
+}
+
+// float(|cl - pt|^2) and float(r(t)^2) exactly as generator.cpp:327-328.
+__device__ __forceinline__ void exact_dist(const SegDev &S, const double pt[3],
+                                           double cl[3], float &dist_squ,
+                                           float &r_sqr) {
+   double t;
+   closest_point(S, pt, cl, t);
+   const double d0 = cl[0] - pt[0], d1 = cl[1] - pt[1], d2 = cl[2] - pt[2];
+   double l2 = 0.0;
+   l2 = l2 + d0 * d0;
+   l2 = l2 + d1 * d1;
+   l2 = l2 + d2 * d2;
+   dist_squ = (float)l2;
+   const double r = S.r0 * (1.0 - t) + S.r1 * t; // fiber.cpp:115-120
+   r_sqr = (float)(r * r);
+}
+
+__global__ void __launch_bounds__(128)
+tissue_keys(const SegDev *__restrict__ segs, int64_t n_segs,
+            const LayerDev *__restrict__ layers, int64_t Y, int64_t Z,
+            unsigned long long *__restrict__ keys,
+            unsigned *__restrict__ min_bundle) {
+   for (int64_t s = blockIdx.x; s < n_segs; s += gridDim.x) {
+      const SegDev &S = segs[s];
+      const float f_ly = layers[S.bundle].f_ly_squ;
+      const int ex = S.ext[0], ey = S.ext[1], ez = S.ext[2];
+      const int plane = ey * ez;
+      const unsigned long long inv_idx =
+          (unsigned long long)(0xFFFFFFFFu - (unsigned)s);
+      const float vfx = S.vf[0], vfy = S.vf[1], vfz = S.vf[2];
+      const float c2f = S.c2f;
+      for (int pl = threadIdx.x; pl < plane; pl += blockDim.x) {
+         const int iy = pl / ez, iz = pl - (pl / ez) * ez;
+         const int64_t y = S.lo[1] + iy, z = S.lo[2] + iz;
+         // FP32 prefilter in segment-local coordinates
+         const float wy = (float)(y - S.base[1]) + (0.5f - S.pf[1]);
+         const float wz = (float)(z - S.base[2]) + (0.5f - S.pf[2]);
+         for (int ix = 0; ix < ex; ix++) {
+            const int64_t x = S.lo[0] + ix;
+            const float wx = (float)(x - S.base[0]) + (0.5f - S.pf[0]);
+            const float c1f = wx * vfx + wy * vfy + wz * vfz;
+            const float w2 = wx * wx + wy * wy + wz * wz;
+            float d2f;
+            if (c1f <= 0.f) {
+               d2f = w2;
+            } else if (c1f >= c2f) {
+               const float ux = wx - vfx, uy = wy - vfy, uz = wz - vfz;
+               d2f = ux * ux + uy * uy + uz * uz;
+            } else {
+               d2f = w2 - c1f * (c1f / c2f);
+            }
+            const float margin = 1e-4f + 3.8e-6f * (w2 + c2f);
+            if (d2f - margin > S.thr_f)
+               continue;
+            // exact reference arithmetic for the survivors
+            const double pt[3] = {(double)x + 0.5, (double)y + 0.5,
+                                  (double)z + 0.5};
+            double cl[3];
+            float dist_squ, r_sqr;
+            exact_dist(S, pt, cl, dist_squ, r_sqr);
+            if (dist_squ > f_ly * r_sqr)
+               continue;
+            const int64_t ind = (x * Y + y) * Z + z;
+            const unsigned long long key =
+                ((unsigned long long)__float_as_uint(dist_squ) << 32) | inv_idx;
+            atomicMin(&keys[ind], key);
+            if (min_bundle)
+               atomicMin(&min_bundle[ind], (unsigned)S.bundle);
+         }
+      }
+   }
+}
+
+__global__ void __launch_bounds__(256)
+tissue_write(const unsigned long long *__restrict__ keys,
+             const SegDev *__restrict__ segs,
+             const LayerDev *__restrict__ layers, int max_layer, int64_t n_vox,
+             int64_t Y, int64_t Z, int32_t *__restrict__ label,
+             float *__restrict__ vec, const unsigned *__restrict__ min_bundle,
+             unsigned long long *__restrict__ counters) {
+   unsigned long long n_overflow = 0, n_overlap = 0;
+   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_vox;
+        i += (int64_t)gridDim.x * blockDim.x) {
+      const unsigned long long key = keys[i];
+      if (key == ~0ull) {
+         label[i] = 0;
+         if (vec) {
+            vec[3 * i + 0] = 0.f;
+            vec[3 * i + 1] = 0.f;
+            vec[3 * i + 2] = 0.f;
+         }
+         continue;
+      }
+      const unsigned seg = 0xFFFFFFFFu - (unsigned)(key & 0xFFFFFFFFull);
+      const float dist_squ = __uint_as_float((unsigned)(key >> 32));
+      const SegDev &S = segs[seg];
+      const LayerDev &L = layers[S.bundle];
+      const int64_t z = i % Z;
+      const int64_t xy = i / Z;
+      const int64_t y = xy % Y;
+      const int64_t x = xy / Y;
+      const double pt[3] = {(double)x + 0.5, (double)y + 0.5, (double)z + 0.5};
+      double cl[3];
+      float d_chk, r_sqr;
+      exact_dist(S, pt, cl, d_chk, r_sqr);
+      // std::lower_bound(scale^2, double(dist_squ / r_sqr)) (generator.cpp:345-349)
+      const double qv = (double)(dist_squ / r_sqr);
+      int ly = 0;
+      while (ly < L.n && L.scale_sq[ly] < qv)
+         ly++;
+      label[i] = ly + 1 + S.bundle * max_layer;
+      if (min_bundle && min_bundle[i] < (unsigned)S.bundle)
+         n_overlap++;
+      if (vec) {
+         double nv[3] = {0.0, 0.0, 0.0};
+         char m = 'b';
+         if (ly < L.n)
+            m = L.model[ly];
+         else
+            n_overflow++;
+         if (m == 'r') {
+            nv[0] = pt[0] - cl[0];
+            nv[1] = pt[1] - cl[1];
+            nv[2] = pt[2] - cl[2];
+         } else if (m == 'p') {
+            nv[0] = S.v[0];
+            nv[1] = S.v[1];
+            nv[2] = S.v[2];
+         }
+         if (m != 'b') { // vm::unit (vemath.hpp:390-402)
+            double n2 = 0.0;
+            n2 = n2 + nv[0] * nv[0];
+            n2 = n2 + nv[1] * nv[1];
+            n2 = n2 + nv[2] * nv[2];
+            if (n2 > 0) {
+               const double inv = 1.0 / sqrt(n2);
+               nv[0] = nv[0] * inv;
+               nv[1] = nv[1] * inv;
+               nv[2] = nv[2] * inv;
+            }
+         }
+         vec[3 * i + 0] = (float)nv[0];
+         vec[3 * i + 1] = (float)nv[1];
+         vec[3 * i + 2] = (float)nv[2];
+      } else if (ly >= L.n) {
+         n_overflow++;
+      }
+   }
+   if (n_overlap)
+      atomicAdd(&counters[0], n_overlap);
+   if (n_overflow)
+      atomicAdd(&counters[5], n_overflow);
+}
+
+// ======================================================================
+// launch
+// ======================================================================
+size_t tissue_workspace_bytes(const TissuePlan &p) {
+   const int64_t nvox = p.X * p.Y * p.Z;
+   size_t b = align_up(sizeof(unsigned long long) * nvox, 256);
+   if (p.n_bundles > 1)
+      b += align_up(sizeof(unsigned) * nvox, 256);
+   b += align_up(sizeof(SegDev) * std::max<size_t>(p.segs.size(), 1), 256);
+   b += align_up(sizeof(LayerDev) * p.layers.size(), 256);
+   b += align_up(sizeof(unsigned long long) * kCounterWords, 256);
+   return b;
+}
+
+int run_tissue(const TissuePlan &p, int only_label, int32_t *d_label,
+               float *d_vector, void *d_ws, size_t ws_bytes,
+               unsigned long long **d_counters_out, cudaStream_t st) {
+   const int64_t nvox = p.X * p.Y * p.Z;
+   const size_t need = tissue_workspace_bytes(p);
+   if (ws_bytes < need) {
+      set_error("generate_tissue: workspace %zu bytes < %zu needed", ws_bytes, need);
+      return FPGB_ENOMEM;
+   }
+   if (reinterpret_cast<uintptr_t>(d_ws) % 256 != 0) {
+      set_error("generate_tissue: workspace must be 256-byte aligned");
+      return FPGB_EINVAL;
+   }
+   char *w = static_cast<char *>(d_ws);
+   auto *keys = reinterpret_cast<unsigned long long *>(w);
+   w += align_up(sizeof(unsigned long long) * nvox, 256);
+   unsigned *minb = nullptr;
+   if (p.n_bundles > 1) {
+      minb = reinterpret_cast<unsigned *>(w);
+      w += align_up(sizeof(unsigned) * nvox, 256);
+   }
+   auto *segs = reinterpret_cast<SegDev *>(w);
+   w += align_up(sizeof(SegDev) * std::max<size_t>(p.segs.size(), 1), 256);
+   auto *layers = reinterpret_cast<LayerDev *>(w);
+   w += align_up(sizeof(LayerDev) * p.layers.size(), 256);
+   auto *counters = reinterpret_cast<unsigned long long *>(w);
+
+   FPGB_CUDA_TRY(cudaMemsetAsync(keys, 0xFF, sizeof(unsigned long long) * nvox, st));
+   if (minb)
+      FPGB_CUDA_TRY(cudaMemsetAsync(minb, 0xFF, sizeof(unsigned) * nvox, st));
+   FPGB_CUDA_TRY(cudaMemsetAsync(counters, 0, sizeof(unsigned long long) * kCounterWords, st));
+   if (!p.segs.empty())
+      FPGB_CUDA_TRY(cudaMemcpyAsync(segs, p.segs.data(), sizeof(SegDev) * p.segs.size(),
+                                    cudaMemcpyHostToDevice, st));
+   FPGB_CUDA_TRY(cudaMemcpyAsync(layers, p.layers.data(), sizeof(LayerDev) * p.layers.size(),
+                                 cudaMemcpyHostToDevice, st));
+   if (!p.segs.empty()) {
+      const int64_t n = (int64_t)p.segs.size();
+      const unsigned grid = (unsigned)std::min<int64_t>(n, 1 << 30);
+      tissue_keys<<<grid, 128, 0, st>>>(segs, n, layers, p.Y, p.Z, keys, minb);
+      FPGB_CUDA_TRY(cudaGetLastError());
+   }
+   {
+      int dev = 0, sms = 0;
+      FPGB_CUDA_TRY(cudaGetDevice(&dev));
+      FPGB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+      const int64_t blocks = std::min<int64_t>((nvox + 255) / 256, (int64_t)sms * 16);
+      tissue_write<<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, st>>>(
+          keys, segs, layers, p.max_layer, nvox, p.Y, p.Z, d_label,
+          only_label ? nullptr : d_vector, minb, counters);
+      FPGB_CUDA_TRY(cudaGetLastError());
+   }
+   if (d_counters_out)
+      *d_counters_out = counters;
+   return FPGB_OK;
+}
+
+static int finish_props(const TissuePlan &p, double *props, int64_t props_cap,
+                        int64_t *n_props) {
+   const int64_t n = (int64_t)p.props.size() / 2;
+   if (n_props)
+      *n_props = n;
+   if (props) {
+      if (props_cap < n) {
+         set_error("props_cap %lld < %lld rows", (long long)props_cap, (long long)n);
+         return FPGB_EINVAL;
+      }
+      std::memcpy(props, p.props.data(), sizeof(double) * 2 * n);
+   }
+   return FPGB_OK;
+}
+
+static int read_tissue_warnings(const TissuePlan &p, unsigned long long *d_counters,
+                                fpgb_warnings *w, cudaStream_t st) {
+   if (!w)
+      return FPGB_OK;
+   long long h[kCounterWords];
+   FPGB_CUDA_TRY(cudaMemcpyAsync(h, d_counters, sizeof h, cudaMemcpyDeviceToHost, st));
+   FPGB_CUDA_TRY(cudaStreamSynchronize(st));
+   warnings_from_counters(h, w);
+   w->overlap = w->overlap > 0 ? 1 : 0; // the reference warns once (generator.cpp:353-359)
+   w->single_point = p.single_point;
+   return FPGB_OK;
+}
+
+} // namespace fpgb
+
+using namespace fpgb;
+
+extern "C" {
+
+size_t fpgb_generate_workspace_size(const fpgb_volume *vol, const fpgb_fibers *fibers) {
+   TissuePlan p;
+   if (plan_tissue(vol, fibers, &p) != FPGB_OK)
+      return 0;
+   return tissue_workspace_bytes(p);
+}
+
+int fpgb_generate_tissue_device(const fpgb_volume *vol, const fpgb_fibers *fibers,
+                                int only_label, int32_t *d_label, float *d_vector,
+                                double *props, int64_t props_cap, int64_t *n_props,
+                                void *d_workspace, size_t workspace_bytes,
+                                fpgb_warnings *warnings, void *stream) {
+   TissuePlan p;
+   FPGB_TRY(plan_tissue(vol, fibers, &p));
+   if (!d_label || (!only_label && !d_vector)) {
+      set_error("generate_tissue_device: null output buffer");
+      return FPGB_EINVAL;
+   }
+   const size_t need = tissue_workspace_bytes(p);
+   if (!d_workspace) {
+      FPGB_TRY(pool_get(kSlotKeys, need, &d_workspace, as_stream(stream)));
+      workspace_bytes = need;
+   }
+   unsigned long long *d_counters = nullptr;
+   cudaStream_t st = as_stream(stream);
+   FPGB_TRY(run_tissue(p, only_label, d_label, d_vector, d_workspace, workspace_bytes,
+                       &d_counters, st));
+   FPGB_TRY(finish_props(p, props, props_cap, n_props));
+   return read_tissue_warnings(p, d_counters, warnings, st);
+}
+
+int fpgb_generate_tissue(const fpgb_volume *vol, const fpgb_fibers *fibers, int only_label,
+                         int32_t *label, float *vector, double *props, int64_t props_cap,
+                         int64_t *n_props, fpgb_warnings *warnings) {
+   TissuePlan p;
+   FPGB_TRY(plan_tissue(vol, fibers, &p));
+   if (!label || (!only_label && !vector)) {
+      set_error("generate_tissue: null output buffer");
+      return FPGB_EINVAL;
+   }
+   const int64_t nvox = p.X * p.Y * p.Z;
+   void *d_label = nullptr, *d_vec = nullptr, *d_ws = nullptr;
+   FPGB_TRY(pool_get(kSlotLabel, sizeof(int32_t) * nvox, &d_label));
+   if (!only_label)
+      FPGB_TRY(pool_get(kSlotVector, sizeof(float) * 3 * nvox, &d_vec));
+   const size_t need = tissue_workspace_bytes(p);
+   FPGB_TRY(pool_get(kSlotKeys, need, &d_ws));
+   cudaStream_t st = nullptr;
+   unsigned long long *d_counters = nullptr;
+   FPGB_TRY(run_tissue(p, only_label, (int32_t *)d_label, (float *)d_vec, d_ws, need,
+                       &d_counters, st));
+   FPGB_CUDA_TRY(cudaMemcpyAsync(label, d_label, sizeof(int32_t) * nvox,
+                                 cudaMemcpyDeviceToHost, st));
+   if (!only_label)
+      FPGB_CUDA_TRY(cudaMemcpyAsync(vector, d_vec, sizeof(float) * 3 * nvox,
+                                    cudaMemcpyDeviceToHost, st));
+   FPGB_TRY(finish_props(p, props, props_cap, n_props));
+   fpgb_warnings tmp;
+   FPGB_TRY(read_tissue_warnings(p, d_counters, warnings ? warnings : &tmp, st));
+   FPGB_CUDA_TRY(cudaStreamSynchronize(st));
+   return FPGB_OK;
+}
+
+} // extern "C"

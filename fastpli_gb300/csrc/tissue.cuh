@@ -1,0 +1,59 @@
+// Voxelizer data layout shared by the plain, batched and no-allocation paths.
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+#include "fpgb_common.cuh"
+
+namespace fpgb {
+
+constexpr int kMaxLayers = 16;
+
+// One fiber segment after translate + resize (voxel units), in the
+// reference's processing order; its table index is the tie-break index.
+struct SegDev {
+   double p[3];   // segment start s0
+   double q[3];   // segment end s1
+   double v[3];   // s1 - s0 (generator.cpp:479)
+   double r0, r1; // radii at s0, s1
+   double c2;     // dot(v, v) (generator.cpp:486)
+   float pf[3];   // p - base, for the FP32 prefilter
+   float vf[3];   // float(v)
+   float c2f;     // float(c2)
+   float thr_f;   // prefilter bound on dist^2 (>= f_ly_squ * max(r0,r1)^2)
+   int32_t base[3]; // floor(p)
+   int32_t lo[3];   // clipped box start (generator.cpp:304)
+   int32_t ext[3];  // clipped box extent
+   int32_t bundle;
+};
+
+// Layers of one bundle, sorted by scale (fiber_bundle.cpp:83-86).
+struct LayerDev {
+   int32_t n = 0;
+   float f_ly_squ = 0.f; // float(scale^2 of the outermost layer)
+   double sqrt_last = 0.0;
+   double scale_sq[kMaxLayers] = {};
+   double dn[kMaxLayers] = {};
+   double mu[kMaxLayers] = {};
+   char model[kMaxLayers] = {};
+};
+
+struct TissuePlan {
+   int64_t X = 0, Y = 0, Z = 0;
+   int64_t n_bundles = 0;
+   int max_layer = 0;
+   int64_t single_point = 0; // fibers skipped with a warning
+   int64_t candidates = 0;   // sum of clipped box volumes
+   std::vector<SegDev> segs;
+   std::vector<LayerDev> layers;
+   std::vector<double> props; // (dn, mu) rows
+};
+
+int plan_tissue(const fpgb_volume *vol, const fpgb_fibers *fb, TissuePlan *plan);
+size_t tissue_workspace_bytes(const TissuePlan &p);
+int run_tissue(const TissuePlan &p, int only_label, int32_t *d_label, float *d_vector,
+               void *d_ws, size_t ws_bytes, unsigned long long **d_counters_out,
+               cudaStream_t st);
+
+} // namespace fpgb

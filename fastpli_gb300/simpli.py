@@ -1,0 +1,361 @@
+"""``Simpli``: the user-facing forward-model API of fastpli on the GPU.
+
+Mirrors the parts of ``fastpli.simulation.Simpli`` that drive the forward
+model (src/fastpli/simulation/simpli.py:18-187 and the property setters of
+src/fastpli/simulation/__simpli.py:97-430): volume and optics properties,
+``generate_tissue()``, ``run_simulation()``, ``apply_epa()`` and
+``memory_usage()``.  The compiled back ends are this package's ``_Generator``
+and ``_Simulator``.  Device-resident helpers (``*_device``) keep the tissue
+in HBM across tilts, which the host API cannot (each reference call re-passes
+the tissue from host memory).
+"""
+
+import warnings
+
+import numpy as np
+
+from . import objects
+from .simulation import _Generator, _Simulator
+
+
+class Simpli:
+    """GPU forward model of 3D-PLI with fastpli's Simpli interface."""
+
+    _FROZEN_OK = True
+
+    def __init__(self, mpi_comm=None):
+        if mpi_comm is not None:
+            raise NotImplementedError("MPI is not supported: one GPU per process")
+        self._dim = None
+        self._dim_origin = np.array([0, 0, 0], dtype=float)
+        self._voxel_size = None
+        self._fiber_bundles = None
+        self._filter_rotations = None
+        self._flip_z_beam = False
+        self._interpolate = "Slerp"
+        self._light_intensity = None
+        self._pixel_size = None
+        self._optical_sigma = None
+        self._step_size = 1.0
+        self._tilts = None
+        self._tissue_refrection = 1.0
+        self._background_absorption = 0.0
+        self._untilt_sensor_view = True
+        self._wavelength = None
+        self._noise_model = None
+        self._omp_num_threads = 1
+        self._verbose = False
+        self._gen = _Generator()
+        self._sim = _Simulator()
+        self._frozen = True
+
+    def __setattr__(self, key, value):
+        if getattr(self, "_frozen", False) and not hasattr(self, key):
+            raise TypeError(f"{self.__class__.__name__} is a frozen class")
+        object.__setattr__(self, key, value)
+
+    # ------------------------------------------------------------ volume ---
+    @property
+    def dim(self):
+        return self._dim
+
+    @dim.setter
+    def dim(self, dim):
+        dim = np.array(dim)
+        if dim.dtype.kind not in "iu":
+            raise TypeError("dim is not np.ndarray(int)")
+        if dim.size != 3:
+            raise TypeError("dim.size != 3")
+        if dim.ndim != 1:
+            raise TypeError("dim.ndim != 1")
+        self._dim = dim.astype(int)
+
+    @property
+    def dim_origin(self):
+        return self._dim_origin
+
+    @dim_origin.setter
+    def dim_origin(self, v):
+        self._dim_origin = np.array(v, dtype=float)
+
+    @property
+    def voxel_size(self):
+        return self._voxel_size
+
+    @voxel_size.setter
+    def voxel_size(self, voxel_size):
+        # __simpli.py:128-143: keeps the VOI when the voxel size changes
+        if voxel_size <= 0:
+            raise ValueError("voxel_size <= 0")
+        keep = self._voxel_size is not None and self._dim is not None
+        if keep:
+            v_min, v_max = self.get_voi()
+        self._voxel_size = float(voxel_size)
+        if keep:
+            self.set_voi(v_min, v_max)
+
+    def get_voi(self):
+        if self._voxel_size is None:
+            raise ValueError("voxel_size is not set, voi can't be calculated")
+        if self._dim is None:
+            raise ValueError("dim is not set, voi can't be calculated")
+        v_min = np.array(self._dim_origin, dtype=float)
+        v_max = v_min + self._dim * self._voxel_size
+        return v_min, v_max
+
+    def set_voi(self, v_min, v_max):
+        v_min = np.array(v_min, dtype=float)
+        v_max = np.array(v_max, dtype=float)
+        if v_min.ndim != 1 or v_max.ndim != 1:
+            raise TypeError("v_min,v_max : ndim != 1")
+        if v_min.size != 3 or v_max.size != 3:
+            raise TypeError("v_min,v_max : size != 1")
+        if np.any(v_min >= v_max):
+            raise ValueError("v_min >= v_max")
+        if self._voxel_size is None:
+            raise TypeError("voxel_size is not set yet")
+        self._dim = np.array(np.round((v_max - v_min) / self._voxel_size), dtype=int)
+        self._dim_origin = v_min
+
+    # ------------------------------------------------------------ optics ---
+    def _scalar(name, conv=float, check=None):
+        def get(self):
+            return getattr(self, "_" + name)
+
+        def set_(self, v):
+            v = conv(v)
+            if check:
+                check(v)
+            object.__setattr__(self, "_" + name, v)
+        return property(get, set_)
+
+    def _positive(name):
+        def check(v):
+            if v <= 0:
+                raise ValueError(f"{name} <= 0")
+        return check
+
+    light_intensity = _scalar("light_intensity")
+    wavelength = _scalar("wavelength")
+    background_absorption = _scalar("background_absorption")
+    tissue_refrection = _scalar("tissue_refrection")
+    step_size = _scalar("step_size")
+    verbose = _scalar("verbose", bool)
+    untilt_sensor_view = _scalar("untilt_sensor_view", bool)
+    flip_z_beam = _scalar("flip_z_beam", bool)
+    pixel_size = _scalar("pixel_size", float, _positive("pixel_size"))
+    omp_num_threads = _scalar("omp_num_threads", int)
+
+    del _scalar, _positive
+
+    @property
+    def filter_rotations(self):
+        return self._filter_rotations
+
+    @filter_rotations.setter
+    def filter_rotations(self, v):
+        v = np.array(v, dtype=float)
+        if v.size == 0 or v.ndim != 1:
+            raise TypeError("filter_rotations : nx1")
+        self._filter_rotations = v
+
+    @property
+    def interpolate(self):
+        return self._interpolate
+
+    @interpolate.setter
+    def interpolate(self, v):
+        if v not in ("NN", "Lerp", "Slerp"):
+            raise ValueError("Only 'NN', 'Lerp' or 'Slerp' are supported")
+        self._interpolate = v
+
+    @property
+    def tilts(self):
+        return self._tilts
+
+    @tilts.setter
+    def tilts(self, tilts):
+        if not isinstance(tilts, (list, tuple, np.ndarray)):
+            raise TypeError("tilts is not a list or array")
+        tilts = np.array(tilts, ndmin=2)
+        if tilts.ndim != 2 or tilts.shape[-1] != 2:
+            raise TypeError("tilts.shape != nx2")
+        self._tilts = tilts
+
+    @property
+    def optical_sigma(self):
+        return self._optical_sigma
+
+    @optical_sigma.setter
+    def optical_sigma(self, v):
+        if not isinstance(v, (int, float)):
+            raise TypeError("optical_sigma is not a number")
+        if v < 0:
+            raise ValueError("optical_sigma is < 0")
+        self._optical_sigma = v
+
+    @property
+    def noise_model(self):
+        return self._noise_model
+
+    @noise_model.setter
+    def noise_model(self, f):
+        if not callable(f):
+            raise TypeError("noise model is not callable")
+        self._noise_model = f
+
+    @property
+    def fiber_bundles(self):
+        return self._fiber_bundles
+
+    @fiber_bundles.setter
+    def fiber_bundles(self, fbs):
+        self._fiber_bundles = None if fbs is None else objects.FiberBundles(fbs)
+
+    def get_dict(self):
+        out = {}
+        for k, v in self.__dict__.items():
+            if k in ("_fiber_bundles", "_gen", "_sim", "_frozen"):
+                continue
+            if k.startswith("_") and not k.startswith("__"):
+                out[k[1:]] = v.tolist() if isinstance(v, np.ndarray) else v
+        return out
+
+    def set_dict(self, data):
+        for k, v in data.items():
+            if k.startswith("_"):
+                raise ValueError("member variable cant be set directly")
+            if v is not None:
+                setattr(self, k, v)
+            else:
+                warnings.warn("None value in dict detected")
+
+    def memory_usage(self, item="all", unit="MB"):
+        """Bytes needed for label + vector (+ distance) per voxel
+        (simpli.py:537-571)."""
+        if self._dim is None:
+            raise ValueError("dim not set")
+        n = float(np.prod(self._dim))
+        per = {"label": 4, "vector": 12, "all": 16 + 8}[item]
+        scale = {"B": 1, "kB": 1e-3, "MB": 1e-6, "GB": 1e-9}[unit]
+        return n * per * scale
+
+    # ------------------------------------------------------------ checks ---
+    def _check_volume_input(self):
+        if self._dim is None:
+            raise ValueError("dim not set")
+        if self._dim_origin is None:
+            raise ValueError("dim_origin not set")
+        if self._voxel_size is None:
+            raise ValueError("voxel_size not set")
+
+    def _check_generation_input(self):
+        if not self._fiber_bundles:
+            raise ValueError("fiber_bundles is not set")
+        for lys in self._fiber_bundles.layers:
+            if lys is None:
+                raise ValueError('fiber_bundle properties are "None"')
+
+    def _check_simulation_input(self):
+        if self._step_size <= 0:
+            raise ValueError("step_size <= 0")
+        if self._light_intensity is None:
+            raise ValueError("light_intensity not set")
+        if self._voxel_size is None:
+            raise ValueError("voxel_size not set")
+        if self._wavelength is None:
+            raise ValueError("wavelength not set")
+        if self._filter_rotations is None:
+            raise ValueError("filter_rotations not set")
+
+    def _init_pli_setup(self):
+        self._check_simulation_input()
+        self._sim.set_pli_setup(self._step_size, self._light_intensity,
+                                self._voxel_size, self._wavelength,
+                                self._tissue_refrection, self._interpolate,
+                                self._untilt_sensor_view, self._flip_z_beam,
+                                self._filter_rotations)
+
+    def _prepare_generator(self):
+        self._check_volume_input()
+        self._check_generation_input()
+        self._gen.set_volume(self._dim, self._dim_origin, self._voxel_size)
+        self._gen.set_fiber_bundles(self._fiber_bundles.as_array(),
+                                    [list(l) for l in self._fiber_bundles.layers])
+
+    # -------------------------------------------------------- forward model ---
+    def generate_tissue(self, only_tissue=False):
+        """simpli.py:61-104 -> (tissue, optical_axis, tissue_properties)."""
+        self._prepare_generator()
+        tissue, optical_axis, props = self._gen.run_generation(only_tissue)
+        props[0, 1] = self._background_absorption
+        if not np.any(tissue):
+            warnings.warn("All labels are 0. Usually this means, that the VOI "
+                          "contains no fiber_bundles or that the voxel_size is to "
+                          "large.", UserWarning)
+        return tissue, optical_axis, props
+
+    def run_simulation(self, tissue, optical_axis, tissue_properties, theta, phi):
+        """simpli.py:125-187 -> images float64 [X, Y, n_rho]."""
+        self._check_volume_input()
+        self._init_pli_setup()
+        tissue_properties = np.array(tissue_properties)
+        if tissue_properties.ndim != 2:
+            raise ValueError("tissue_properties.ndim !=2")
+        if tissue_properties.shape[1] != 2:
+            raise ValueError("tissue_properties.shape[1] != 2")
+        tissue = np.asarray(tissue)
+        optical_axis = np.asarray(optical_axis)
+        if tissue.ndim != 3:
+            raise ValueError("tissue.ndim != 3")
+        if optical_axis.ndim != 4:
+            raise ValueError("optical_axis.ndim != 4")
+        if optical_axis.shape[3] != 3:
+            raise ValueError("optical_axis.shape[3] != 3")
+        if tuple(tissue.shape) != tuple(optical_axis.shape[:-1]):
+            raise ValueError("not np.equal(tissue.shape, optical_axis.shape[:-1])")
+        if tissue.dtype != np.int32:
+            warnings.warn("tissue is copied", UserWarning)
+        if optical_axis.dtype != np.float32:
+            warnings.warn("optical_axis is copied", UserWarning)
+        images = self._sim.run_simulation(self._dim, tissue, optical_axis,
+                                          tissue_properties, theta, phi)
+        if np.min(images.flatten()) < 0:
+            raise ValueError("intensity < 0 detected")
+        return images
+
+    def apply_epa(self, data, mask=None):
+        """__simpli.py:597-621: transmittance, direction, retardation."""
+        from . import analysis
+        t, d, r = analysis.epa(data)
+        if mask is not None:
+            t[~mask], d[~mask], r[~mask] = 0, 0, 0
+        return t, d, r
+
+    # ------------------------------------------------- device-resident path ---
+    def generate_tissue_device(self, only_tissue=False, stream=None):
+        """Voxelize into HBM: (label, vector) torch CUDA tensors + props."""
+        self._prepare_generator()
+        label, vector, props, _ = self._gen.run_generation_device(only_tissue, stream)
+        props = props.copy()
+        props[0, 1] = self._background_absorption
+        return label, vector, props
+
+    def run_simulation_device(self, label, vector, tissue_properties, theta, phi,
+                              epa=False, stream=None):
+        """March device-resident tissue (no host copies)."""
+        self._check_volume_input()
+        self._init_pli_setup()
+        return self._sim.run_simulation_device(self._dim, label, vector,
+                                               tissue_properties, theta, phi,
+                                               epa=epa, stream=stream)
+
+    def run_tilts_device(self, label, vector, tissue_properties, tilts=None,
+                         epa=False, stream=None):
+        """All tilts of ``self.tilts`` on resident tissue -> list of results."""
+        tilts = self._tilts if tilts is None else np.array(tilts, ndmin=2)
+        if tilts is None:
+            raise ValueError("tilts not set")
+        return [self.run_simulation_device(label, vector, tissue_properties,
+                                           float(t), float(p), epa=epa, stream=stream)
+                for t, p in tilts]

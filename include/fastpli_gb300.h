@@ -1,0 +1,164 @@
+/*
+ * fastpli_gb300 — C ABI of the GB300 (sm_103a) forward model of 3D-PLI.
+ *
+ * Drop-in for the two pybind11 classes fastpli's `Simpli` binds:
+ *   _Generator  (src/simulation/bindings/generator_module.cpp:23-140)
+ *   _Simulator  (src/simulation/bindings/simulator_module.cpp:18-157)
+ * Every entry point takes plain pointers and sizes; streams are passed as
+ * `void *` holding a cudaStream_t (NULL = legacy default stream).  Calls
+ * return 0 on success or a negative FPGB_E* code; fpgb_last_error() then
+ * holds the message (thread-local).  Argument errors the reference raises as
+ * std::invalid_argument / ValueError, and the input checks it answers with
+ * exit(EXIT_FAILURE) (src/simulation/simulator.cpp:62-69,131-176), are both
+ * reported as FPGB_EINVAL here — nothing in this library exits the process.
+ *
+ * Units and layouts are the reference's: lengths in µm, wavelength in nm,
+ * angles in rad; label [X][Y][Z] int32 and vector [X][Y][Z][3] float32,
+ * z fastest; images [X][Y][n_rho] float64.
+ */
+#ifndef FASTPLI_GB300_H_
+#define FASTPLI_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FPGB_OK 0
+#define FPGB_EINVAL (-1)   /* invalid argument / inconsistent input */
+#define FPGB_ECUDA (-2)    /* CUDA runtime error */
+#define FPGB_ENOMEM (-3)   /* allocation failed / workspace too small */
+#define FPGB_ETIMEOUT (-4) /* a bounded device wait gave up */
+
+/* Counters of the reference's Python UserWarnings (PyErr_WarnEx sites). */
+typedef struct fpgb_warnings {
+   int64_t overlap;        /* "objects overlap" generator.cpp:357 */
+   int64_t single_point;   /* "fiber object with only single point" :215 */
+   int64_t zero_axis;      /* "optical_axis is 0 for tissue > 0" simulator.cpp:294 */
+   int64_t not_normalized; /* "optical_axis not normalized" simulator.cpp:300 */
+   int64_t empty_light;    /* "light_positions is empty" simulator.cpp:715 */
+   int64_t layer_overflow; /* voxels whose layer quotient lies beyond the
+                              outermost layer (generator.cpp:345-366 reads past
+                              its layer table there; here: zero vector) */
+} fpgb_warnings;
+
+/* Volume of _Generator.set_volume (generator_module.cpp:29-35,
+ * generator.cpp:45-124). */
+typedef struct fpgb_volume {
+   int64_t dim[3];
+   double origin[3];
+   double voxel_size;
+} fpgb_volume;
+
+/* Fiber bundles of _Generator.set_fiber_bundles (generator_module.cpp:37-66)
+ * flattened: fiber f owns points [fiber_point_off[f], fiber_point_off[f+1]),
+ * bundle b owns fibers [bundle_fiber_off[b], bundle_fiber_off[b+1]) and
+ * layers [bundle_layer_off[b], bundle_layer_off[b+1]).  Host memory. */
+typedef struct fpgb_fibers {
+   int64_t n_bundles;
+   const int64_t *bundle_fiber_off; /* [n_bundles + 1] */
+   const int64_t *fiber_point_off;  /* [n_fibers + 1] */
+   const double *points;            /* [n_points][4] = x, y, z, radius */
+   const int64_t *bundle_layer_off; /* [n_bundles + 1] */
+   const double *layer_scale;       /* [n_layers] */
+   const double *layer_dn;
+   const double *layer_mu;
+   const char *layer_model; /* 'b' background, 'p' parallel, 'r' radial */
+} fpgb_fibers;
+
+/* _Simulator.set_pli_setup (simulator_module.cpp:23-54, setup.hpp:47-82). */
+typedef struct fpgb_setup {
+   double step_size;       /* in voxels */
+   double light_intensity; /* a.u. */
+   double voxel_size;      /* µm */
+   double wavelength;      /* nm */
+   double tissue_refrection;
+   int32_t interpolate; /* 0 = NN, 1 = Lerp, 2 = Slerp */
+   int32_t untilt_sensor_view;
+   int32_t flip_z;
+   int32_t n_rho;
+   const double *filter_rotations; /* [n_rho], host memory, rad */
+} fpgb_setup;
+
+const char *fpgb_last_error(void);
+const char *fpgb_version(void);
+
+/* ----------------------------------------------------------------------------
+ * Voxelizer.  Replaces _Generator.run_generation
+ * (generator_module.cpp:99-134 -> PliGenerator::RunTissueGeneration,
+ * generator.cpp:163-261).  n_props = 1 + n_bundles * max_layer rows of
+ * (dn, mu) (generator.cpp:496-526); row 0 is (0, 0).
+ * -------------------------------------------------------------------------- */
+
+/* Host buffers in and out (copies inside): label [X*Y*Z], vector
+ * [X*Y*Z*3] (unused when only_label), props [props_cap][2]. */
+int fpgb_generate_tissue(const fpgb_volume *vol, const fpgb_fibers *fibers,
+                         int only_label, int32_t *label, float *vector,
+                         double *props, int64_t props_cap, int64_t *n_props,
+                         fpgb_warnings *warnings);
+
+/* Device-resident variant.  d_label / d_vector are device buffers of the
+ * full volume; d_workspace (>= fpgb_generate_workspace_size bytes, 256-byte
+ * aligned) holds the per-voxel keys and the segment table, or NULL to use the
+ * library's own cached device pool.  props/n_props/warnings are host memory;
+ * warnings != NULL synchronises the stream. */
+size_t fpgb_generate_workspace_size(const fpgb_volume *vol,
+                                    const fpgb_fibers *fibers);
+int fpgb_generate_tissue_device(const fpgb_volume *vol,
+                                const fpgb_fibers *fibers, int only_label,
+                                int32_t *d_label, float *d_vector,
+                                double *props, int64_t props_cap,
+                                int64_t *n_props, void *d_workspace,
+                                size_t workspace_bytes, fpgb_warnings *warnings,
+                                void *stream);
+
+/* ----------------------------------------------------------------------------
+ * Ray march.  Replaces _Simulator.run_simulation
+ * (simulator_module.cpp:61-93 -> PliSimulator::RunSimulation,
+ * simulator.cpp:182-411).
+ * -------------------------------------------------------------------------- */
+
+/* Host buffers in and out: label [X*Y*Z], vector [X*Y*Z*3], props
+ * [n_props][2] (dn, mu) -> image [X*Y*n_rho] float64. */
+int fpgb_run_simulation(const fpgb_setup *setup, const int64_t *dim,
+                        const int32_t *label, const float *vector,
+                        const double *props, int64_t n_props, double theta,
+                        double phi, double *image, fpgb_warnings *warnings);
+
+/* Device-resident variant: d_label, d_vector, d_image on the device; props
+ * on the host (a small table, copied into the launch).  Label range checks
+ * (simulator.cpp:149-167) run on the device.  warnings != NULL synchronises;
+ * with NULL the call is fully asynchronous and range errors are reported by
+ * the next synchronising call on that stream. */
+int fpgb_run_simulation_device(const fpgb_setup *setup, const int64_t *dim,
+                               const int32_t *d_label, const float *d_vector,
+                               const double *props, int64_t n_props,
+                               double theta, double phi, double *d_image,
+                               fpgb_warnings *warnings, void *stream);
+
+/* Same march, with the epa modalities of fastpli.analysis.epa.epa
+ * (src/fastpli/analysis/epa.py:9-45) fused into the epilogue: d_trans,
+ * d_dir, d_ret are [X*Y] float64 (any may be NULL). */
+int fpgb_run_simulation_epa_device(const fpgb_setup *setup, const int64_t *dim,
+                                   const int32_t *d_label,
+                                   const float *d_vector, const double *props,
+                                   int64_t n_props, double theta, double phi,
+                                   double *d_image, double *d_trans,
+                                   double *d_dir, double *d_ret,
+                                   fpgb_warnings *warnings, void *stream);
+
+/* Number of ray-voxel steps one run_simulation call marches: X*Y rays times
+ * the steps each takes (simulator.cpp:259-261), computed on the host. */
+int64_t fpgb_count_steps(const fpgb_setup *setup, const int64_t *dim,
+                         double theta, double phi);
+
+/* Release the library's cached device pool on the current device. */
+int fpgb_release_pool(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FASTPLI_GB300_H_ */

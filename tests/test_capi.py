@@ -1,0 +1,113 @@
+"""C-ABI checks that need no GPU: the library builds, loads and exports every
+symbol the header declares; host-side planning and argument validation."""
+
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import fastpli_gb300
+from fastpli_gb300 import _native as N
+from fastpli_gb300.simulation import _Generator, _Simulator
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    src = open(os.path.join(ROOT, "include", "fastpli_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(fpgb_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_loads_and_exports_header_symbols():
+    lib = fastpli_gb300.native_library()
+    names = header_functions()
+    assert len(names) >= 10
+    for n in names:
+        assert hasattr(lib, n), f"{n} declared in include/ but not exported"
+    assert set(names) == set(N.exported_symbols()), "ctypes table out of sync with header"
+    assert b"sm_103a" in lib.fpgb_version()
+
+
+def _setup(**kw):
+    base = dict(step_size=1.0, light_intensity=26000.0, voxel_size=0.2, wavelength=525.0,
+                tissue_refrection=1.0, interpolate="Slerp", untilt_sensor_view=True,
+                flip_z=False, filter_rotations=np.deg2rad(np.arange(0, 180, 20)))
+    base.update(kw)
+    return N.SetupBlock(**base)
+
+
+def _steps_reference_loop(Z, theta, phi, step):
+    """Replays simulator.cpp:230-231,259-261 for the z coordinate."""
+    dz = np.cos(theta) * step if theta != 0 else step
+    z, n = 0.0 + dz * 0.5, 0
+    while 0 <= np.floor(z) < Z:
+        n += 1
+        z = z + dz
+    return n
+
+
+@pytest.mark.parametrize("theta,step", [(0.0, 1.0), (np.deg2rad(5.5), 1.0),
+                                        (np.deg2rad(30), 0.37), (0.0, 2.5)])
+def test_count_steps_matches_reference_loop(theta, step):
+    s = _setup(step_size=step)
+    dim = np.array([7, 5, 120], np.int64)
+    n = N.load().fpgb_count_steps(N.byref(s.struct), N.ptr(dim), theta, 0.3)
+    assert n == 7 * 5 * _steps_reference_loop(120, theta, 0.3, step)
+
+
+@pytest.mark.parametrize("bad,msg", [
+    (dict(step_size=0.0), "step_size"), (dict(light_intensity=-1.0), "light"),
+    (dict(voxel_size=0.0), "voxel_size"), (dict(wavelength=0.0), "wavelength"),
+    (dict(tissue_refrection=0.5), "tissue_refrection"),
+    (dict(filter_rotations=[]), "filter_rotations")])
+def test_setup_validation_raises_before_any_device_work(bad, msg):
+    sim = _Simulator()
+    kw = dict(step_size=1.0, light_intensity=1.0, voxel_size=1.0, wavelength=525.0,
+              tissue_refrection=1.0, interpolate="NN", untilt_sensor_view=True, flip_z=False,
+              filter_rotations=[0.0])
+    kw.update(bad)
+    sim.set_pli_setup(**kw)
+    lab = np.zeros((2, 2, 2), np.int32)
+    vec = np.zeros((2, 2, 2, 3), np.float32)
+    with pytest.raises(ValueError, match=msg):
+        sim.run_simulation([2, 2, 2], lab, vec, np.zeros((1, 2)), 0.0, 0.0)
+
+
+def test_interpolate_string_checked():
+    with pytest.raises(ValueError, match="NN, Lerp or Slerp"):
+        _Simulator().set_pli_setup(1, 1, 1, 525, 1, "Cubic", True, False, [0.0])
+
+
+def test_background_birefringence_rejected():
+    sim = _Simulator()
+    sim.set_pli_setup(1, 1, 1, 525, 1, "NN", True, False, [0.0])
+    with pytest.raises(ValueError, match="background birefringence"):
+        sim.run_simulation([1, 1, 1], np.zeros((1, 1, 1), np.int32),
+                           np.zeros((1, 1, 1, 3), np.float32), np.array([[0.1, 0.0]]), 0, 0)
+
+
+def test_generator_volume_validation():
+    g = _Generator()
+    with pytest.raises(ValueError, match="dim.global"):
+        g.set_volume([0, 4, 4], [0, 0, 0], 1.0)
+    with pytest.raises(ValueError, match="voxel_size"):
+        g.set_volume([4, 4, 4], [0, 0, 0], 0.0)
+    with pytest.raises(ValueError, match="Orientation"):
+        g.set_fiber_bundles([[np.zeros((2, 4))]], [[(1.0, 0.0, 0.0, "x")]])
+    with pytest.raises(ValueError, match="not the same size"):
+        g.set_fiber_bundles([[np.zeros((2, 4))]], [])
+
+
+def test_workspace_size_is_host_planned():
+    g = _Generator()
+    g.set_volume([10, 12, 14], [0, 0, 0], 0.5)
+    g.set_fiber_bundles([[np.array([[0, 0, 0, 1], [5, 6, 7, 1]], float)],
+                         [np.array([[5, 0, 0, 1], [5, 6, 7, 1.5]], float)]],
+                        [[(1.0, 0.004, 1.0, "r")], [(0.5, 0.0, 1.0, "b"), (1.0, 0.004, 1.0, "p")]])
+    n = 10 * 12 * 14
+    ws = g.workspace_size()
+    assert ws >= 8 * n + 4 * n  # keys + per-voxel bundle minimum (two bundles)
+    assert g.n_props() == 1 + 2 * 2
