@@ -194,6 +194,11 @@ int plan_tissue(const fpgb_volume *vol, const fpgb_fibers *fb, TissuePlan *plan)
    const bool translate =
        vol->origin[0] != 0 || vol->origin[1] != 0 || vol->origin[2] != 0;
    const double f = 1.0 / vol->voxel_size;
+   for (int64_t i = 0; i < 4 * np; i++)
+      if (!std::isfinite(fb->points[i])) {
+         set_error("fiber point %lld is not finite", (long long)(i / 4));
+         return FPGB_EINVAL;
+      }
    for (int64_t i = 0; i < np; i++) {
       for (int c = 0; c < 3; c++) {
          double v = fb->points[4 * i + c];
@@ -256,8 +261,16 @@ int plan_tissue(const fpgb_volume *vol, const fpgb_fibers *fb, TissuePlan *plan)
                   sb.mn[i] = volbox.mn[i];
                if (volbox.mx[i] < sb.mx[i])
                   sb.mx[i] = volbox.mx[i];
-               const int64_t lo = (int64_t)sb.mn[i];
-               const int64_t hi = (int64_t)(sb.mx[i] + 0.5);
+               if (!(sb.mn[i] <= sb.mx[i])) { // empty or non-finite box
+                  count = 0;
+                  S.lo[i] = 0;
+                  S.ext[i] = 0;
+                  continue;
+               }
+               // (int64) truncation as generator.cpp:304-305; the clamp only
+               // restates that the box already lies in [0, dim]
+               const int64_t lo = std::max<int64_t>(0, (int64_t)sb.mn[i]);
+               const int64_t hi = std::min<int64_t>(vol->dim[i], (int64_t)(sb.mx[i] + 0.5));
                S.lo[i] = (int32_t)lo;
                S.ext[i] = (int32_t)(hi > lo ? hi - lo : 0);
                count *= S.ext[i];

@@ -185,8 +185,12 @@ def test_device_path_and_fused_epa(cuda, oracle_port):
         et, ed, er = oracle_port.epa(ref[k])
         trel = _rel(tt.cpu().numpy(), et)
         rrel = float(np.max(np.abs(rr.cpu().numpy() - er) / np.maximum(np.abs(er), 1e-3)))
-        dd_ = np.abs(dd.cpu().numpy() - ed)
-        derr = float(np.max(np.minimum(dd_, np.pi - dd_)))
+        # direction is only defined where the pixel has retardation: on
+        # uniform (background) pixels a1 = b1 = 0 up to rounding and
+        # atan2 returns noise in both implementations
+        defined = er > 1e-2
+        dd_ = np.abs(dd.cpu().numpy() - ed)[defined]
+        derr = float(np.max(np.minimum(dd_, np.pi - dd_))) if dd_.size else 0.0
         REPORT[f"epa/{name}/{k}"] = {"t_rel": trel, "r_rel": rrel, "d_abs": derr}
         assert trel <= EPA_TOL and rrel <= EPA_TOL and derr <= EPA_TOL
 
