@@ -277,15 +277,15 @@ int plan_march(const fpgb_setup *s, const int64_t *dim, const double *props, int
    P.dx_fx = std::llrint(std::ldexp(step[0], P.frac_bits));
    P.dy_fx = std::llrint(std::ldexp(step[1], P.frac_bits));
 
-   P.i4 = s->light_intensity / 4.0;
+   P.i4 = (float)(s->light_intensity / 4.0);
    const int n = s->n_rho;
    for (int r = 0; r < n; r++) {
-      P.c2r[r] = std::cos(2.0 * s->filter_rotations[r]);
-      P.s2r[r] = std::sin(2.0 * s->filter_rotations[r]);
+      P.c2r[r] = (float)std::cos(2.0 * s->filter_rotations[r]);
+      P.s2r[r] = (float)std::sin(2.0 * s->filter_rotations[r]);
       // rho_2 = 2 * linspace(0, pi, n, endpoint=False) (epa.py:29)
       const double rho2 = 2.0 * (M_PI / n * r);
-      P.epa_sin[r] = std::sin(rho2);
-      P.epa_cos[r] = std::cos(rho2);
+      P.epa_sin[r] = (float)std::sin(rho2);
+      P.epa_cos[r] = (float)std::cos(rho2);
    }
    return FPGB_OK;
 }
@@ -318,8 +318,22 @@ __device__ __forceinline__ F3 lerp_axis(F3 v, F3 u, float t) {
    return F3{a.x - b.x, a.y - b.y, a.z - b.z};
 }
 
-// SphericalInterpolation (simulator.cpp:473-494) in FP32.  Below the FP32
-// resolution of the angle the weights tend to (1 - t, t).
+// sin(sqrt(y)) / sqrt(y) by its Taylor series in y = x^2, truncated after
+// y^5 (remainder < y^6 / 13! <= 4e-13 for y <= 0.36)
+__device__ __forceinline__ float sinc_sq(float y) {
+   float p = -1.f / 39916800.f;
+   p = fmaf(p, y, 1.f / 362880.f);
+   p = fmaf(p, y, -1.f / 5040.f);
+   p = fmaf(p, y, 1.f / 120.f);
+   p = fmaf(p, y, -1.f / 6.f);
+   return fmaf(p, y, 1.f);
+}
+
+// SphericalInterpolation (simulator.cpp:473-494) in FP32.  The weights
+// sin((1-t)th)/sin(th) and sin(t th)/sin(th) are evaluated as
+// (1-t) S((1-t)^2 th^2) / S(th^2) and t S(t^2 th^2) / S(th^2), S(y) =
+// sin(sqrt y)/sqrt y, for th < 0.6 (smooth fibre fields), which needs no
+// sine calls and stays accurate as th -> 0; larger angles use sinf.
 __device__ __forceinline__ F3 slerp_axis(F3 v, F3 u, float t) {
    if (is_zero(v))
       return u;
@@ -335,13 +349,14 @@ __device__ __forceinline__ F3 slerp_axis(F3 v, F3 u, float t) {
       return v;
    const float c = fminf(d * rsqrtf(dot3(v, v) * dot3(u, u)), 1.f);
    const float th = acosf(c);
-   const float sth = sinf(th);
    float w0, w1;
-   if (sth < 1e-6f) {
-      w0 = 1.f - t;
-      w1 = t;
+   if (th < 0.6f) {
+      const float y = th * th, s = 1.f - t;
+      const float inv = __fdividef(1.f, sinc_sq(y));
+      w0 = s * sinc_sq(s * s * y) * inv;
+      w1 = t * sinc_sq(t * t * y) * inv;
    } else {
-      const float inv = 1.f / sth;
+      const float inv = __fdividef(1.f, sinf(th));
       w0 = sinf((1.f - t) * th) * inv;
       w1 = sinf(t * th) * inv;
    }
@@ -384,11 +399,17 @@ __device__ F3 axis_interp(const MarchParams &P, const int32_t *__restrict__ labe
       z1 = P.Z - 1 - z1;
    }
    const int64_t YZ = P.Y * P.Z;
-   if (x0 == x1 && y0 == y1 && z0 == z1)
+   const bool ax = x0 != x1, ay = y0 != y1, az = z0 != z1;
+   if (!ax && !ay && !az)
       return load_vec(vec, x0 * YZ + y0 * P.Z + z0);
+   // Corners along a collapsed axis coincide, and interpolating a vector
+   // with itself returns it unchanged (both the reference's Lerp and Slerp),
+   // so collapsed levels are skipped without changing the result.
    F3 c[8];
 #pragma unroll
    for (int k = 0; k < 8; k++) {
+      if (((k & 1) && !ax) || ((k & 2) && !ay) || ((k & 4) && !az))
+         continue;
       const int64_t xi = (k & 1) ? x1 : x0, yi = (k & 2) ? y1 : y0, zi = (k & 4) ? z1 : z0;
       const int64_t idx = xi * YZ + yi * P.Z + zi;
       if (__ldg(label + idx) == lab)
@@ -396,13 +417,26 @@ __device__ F3 axis_interp(const MarchParams &P, const int32_t *__restrict__ labe
       else
          c[k] = F3{0.f, 0.f, 0.f};
    }
-   const F3 c00 = interp_axis<MODE>(c[0], c[1], xd);
-   const F3 c01 = interp_axis<MODE>(c[4], c[5], xd);
-   const F3 c10 = interp_axis<MODE>(c[2], c[3], xd);
-   const F3 c11 = interp_axis<MODE>(c[6], c[7], xd);
-   const F3 c0 = interp_axis<MODE>(c00, c10, yd);
-   const F3 c1 = interp_axis<MODE>(c01, c11, yd);
-   return interp_axis<MODE>(c0, c1, zd);
+   F3 c00 = c[0], c10 = c[2], c01 = c[4], c11 = c[6];
+   if (ax) {
+      c00 = interp_axis<MODE>(c[0], c[1], xd);
+      if (az)
+         c01 = interp_axis<MODE>(c[4], c[5], xd);
+      if (ay) {
+         c10 = interp_axis<MODE>(c[2], c[3], xd);
+         if (az)
+            c11 = interp_axis<MODE>(c[6], c[7], xd);
+      }
+   }
+   F3 c0 = c00, c1 = c01;
+   if (ay) {
+      c0 = interp_axis<MODE>(c00, c10, yd);
+      if (az)
+         c1 = interp_axis<MODE>(c01, c11, yd);
+   }
+   if (az)
+      return interp_axis<MODE>(c0, c1, zd);
+   return c0;
 }
 
 // Ray start in the reference's double operation order
@@ -450,6 +484,26 @@ __device__ __forceinline__ int64_t to_fixed(double v, int frac_bits) {
    return i * (int64_t(1) << frac_bits) + f;
 }
 
+// sin and cos of a small angle by their Taylor series (|x| <= 0.25:
+// remainders below x^9/9! and x^10/10!, under 1e-11); larger angles use
+// sincosf.
+__device__ __forceinline__ void sincos_small(float x, float &s, float &c) {
+   if (fabsf(x) <= 0.25f) {
+      const float y = x * x;
+      float ps = -1.f / 5040.f;
+      ps = fmaf(ps, y, 1.f / 120.f);
+      ps = fmaf(ps, y, -1.f / 6.f);
+      s = fmaf(ps * y, x, x);
+      float pc = 1.f / 40320.f;
+      pc = fmaf(pc, y, -1.f / 720.f);
+      pc = fmaf(pc, y, 1.f / 24.f);
+      pc = fmaf(pc, y, -0.5f);
+      c = fmaf(pc, y, 1.f);
+   } else {
+      sincosf(x, &s, &c);
+   }
+}
+
 // One birefringent step on the unit state (u1, u2, u3).
 __device__ __forceinline__ void retard(float &u1, float &u2, float &u3, F3 v, float n2,
                                        float kret) {
@@ -458,8 +512,8 @@ __device__ __forceinline__ void retard(float &u1, float &u2, float &u3, F3 v, fl
    if (q > 0.f) {
       const float ret = kret * q * rsqrtf(n2);
       float sr, cr;
-      sincosf(ret, &sr, &cr);
-      const float iq = 1.f / q;
+      sincos_small(ret, sr, cr);
+      const float iq = __fdividef(1.f, q);
       const float c = (xx - yy) * iq, s = 2.f * v.x * v.y * iq;
       const float a1 = u1 * c - u2 * s;
       const float c1 = u1 * s + u2 * c;
@@ -541,30 +595,34 @@ march_rays(const MarchParams P, const int32_t *__restrict__ label,
       L += o.alog;
    }
    // analyser and the rho epilogue (simulator.cpp:346-362)
-   const double amp = P.i4 * exp(-(double)L);
-   double a0 = 0, a1 = 0, b1 = 0;
+   const float amp = P.i4 * expf(-L);
+   float a0 = 0.f, a1 = 0.f, b1 = 0.f;
    double *out = image + ray * P.n_rho;
    for (int r = 0; r < P.n_rho; r++) {
-      const double I = amp * (1.0 - (double)u1 * P.c2r[r] + (double)u2 * P.s2r[r]);
+      const float I = amp * (1.f - u1 * P.c2r[r] + u2 * P.s2r[r]);
       if (image)
-         out[r] = I;
+         out[r] = (double)I;
       a0 += I;
       a1 += I * P.epa_sin[r];
       b1 += I * P.epa_cos[r];
    }
    if (epa_t || epa_d || epa_r) { // epa.py:31-43
-      const double n = (double)P.n_rho;
+      const float n = (float)P.n_rho;
       a0 = a0 / n;
-      a1 = 2.0 * a1 / n;
-      b1 = 2.0 * b1 / n;
+      a1 = 2.f * a1 / n;
+      b1 = 2.f * b1 / n;
       if (epa_t)
-         epa_t[ray] = 2.0 * a0;
-      if (epa_d)
-         epa_d[ray] = fmod(0.5 * atan2(-b1, a1) + M_PI, M_PI);
+         epa_t[ray] = 2.0 * (double)a0;
+      if (epa_d) {
+         float d = 0.5f * atan2f(-b1, a1) + 3.14159265358979f;
+         if (d >= 3.14159265358979f)
+            d -= 3.14159265358979f;
+         epa_d[ray] = (double)d;
+      }
       if (epa_r) {
-         if (a0 < 2.220446049250313e-16 * 100)
-            a0 = 1.0;
-         epa_r[ray] = sqrt(a1 * a1 + b1 * b1) / a0;
+         if ((double)a0 < 2.220446049250313e-16 * 100)
+            a0 = 1.f;
+         epa_r[ray] = (double)(sqrtf(a1 * a1 + b1 * b1) / a0);
       }
    }
    if (w_zero)

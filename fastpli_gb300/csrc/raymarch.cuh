@@ -41,9 +41,9 @@ struct MarchParams {
    double A, B, C, Dd, D; // tilted-view 2x2 system (simulator.cpp:653-668)
    double rti[9];         // inverse tissue rotation (simulator.cpp:636-638)
    float rot[9];          // RotZYZ(phi, theta, -phi) for the optic axis
-   double i4;             // light_intensity / 4
-   double c2r[kMaxRho], s2r[kMaxRho]; // cos 2rho, sin 2rho of the filter angles
-   double epa_sin[kMaxRho], epa_cos[kMaxRho]; // sin/cos(2*pi*i/n) of epa.py:29
+   float i4;              // light_intensity / 4
+   float c2r[kMaxRho], s2r[kMaxRho]; // cos 2rho, sin 2rho of the filter angles
+   float epa_sin[kMaxRho], epa_cos[kMaxRho]; // sin/cos(2*pi*i/n) of epa.py:29
    const LabelOptics *lut;
    const ZStep *ztab;
 };

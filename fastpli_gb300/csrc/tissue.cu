@@ -29,8 +29,10 @@
 #include <cstring>
 #include <vector>
 
+#include "ff.cuh"
 #include "fpgb_common.cuh"
 #include "tissue.cuh"
+#include "tissue_eval.cuh"
 
 namespace fpgb {
 
@@ -96,6 +98,55 @@ Box fiber_box(const double *xyz, const double *r, int64_t n) {
       b.unite(t);
    }
    return b;
+}
+
+// double -> (hi, lo) float pair; |d - hi - lo| <= 2^-48 |d|
+void split2(double d, float &hi, float &lo) {
+   hi = (float)d;
+   lo = (float)(d - (double)hi);
+}
+
+// Host-side constants of the two-float path, all derived in double exactly
+// as the reference derives the corresponding values.
+void fill_fast_fields(SegDev &S, const fpgb_volume *vol) {
+   double ps = 0;
+   for (int i = 0; i < 3; i++) {
+      split2(S.p[i] - (double)S.base[i], S.pl_hi[i], S.pl_lo[i]);
+      split2(S.v[i], S.v_hi[i], S.v_lo[i]);
+      ps = std::max(ps, std::max(std::fabs(S.p[i]), std::fabs(S.q[i])));
+      ps = std::max(ps, (double)vol->dim[i]);
+   }
+   S.pscale = (float)(ps + 2.0);
+   split2(S.c2, S.c2_hi, S.c2_lo);
+   split2(S.r0, S.r0_hi, S.r0_lo);
+   split2(S.r1 - S.r0, S.dr_hi, S.dr_lo);
+   // Fiber::CalcRadius at t = 0 and t = 1 is exactly r0 and r1
+   // (fiber.cpp:115-120): r0*(1-0) + r1*0 = r0, r0*0 + r1*1 = r1
+   S.rsq0 = (float)(S.r0 * S.r0);
+   S.rsq1 = (float)(S.r1 * S.r1);
+   // r0 == r1: every interior r(t) is r0 within a few ulp, so float(r^2) is
+   // fixed unless r0^2 sits next to a float rounding boundary
+   S.rsq_const = NAN;
+   if (S.r0 == S.r1) {
+      const double r2 = S.r0 * S.r0;
+      const double eps = 64.0 * 0x1p-53;
+      const float a = (float)(r2 * (1.0 - eps)), b = (float)(r2 * (1.0 + eps));
+      if (a == b)
+         S.rsq_const = a;
+   }
+   // 'p' layer vector: vm::unit(q - p) (generator.cpp:372-373, vemath.hpp:390-402)
+   double n2 = 0.0;
+   n2 = n2 + S.v[0] * S.v[0];
+   n2 = n2 + S.v[1] * S.v[1];
+   n2 = n2 + S.v[2] * S.v[2];
+   double u[3] = {S.v[0], S.v[1], S.v[2]};
+   if (n2 > 0) {
+      const double inv = 1.0 / std::sqrt(n2);
+      for (int i = 0; i < 3; i++)
+         u[i] = u[i] * inv;
+   }
+   for (int i = 0; i < 3; i++)
+      S.vp[i] = (float)u[i];
 }
 
 } // namespace
@@ -296,6 +347,7 @@ int plan_tissue(const fpgb_volume *vol, const fpgb_fibers *fb, TissuePlan *plan)
             S.c2f = (float)S.c2;
             S.r0 = r0;
             S.r1 = r1;
+            fill_fast_fields(S, vol);
             const double rm = r0 < r1 ? r1 : r0;
             S.thr_f = (float)((double)L.f_ly_squ * rm * rm * (1.0 + 1e-3) + 1e-3);
             S.bundle = (int32_t)b;
@@ -316,56 +368,12 @@ int plan_tissue(const fpgb_volume *vol, const fpgb_fibers *fb, TissuePlan *plan)
 // device code
 // ======================================================================
 
-// Closest point of `pt` on segment S and its parameter t, in the reference's
-// double operation order (generator.cpp:475-494).  -fmad=false keeps every
-// product and sum separately rounded.
-__device__ __forceinline__ void closest_point(const SegDev &S, const double pt[3],
-                                              double cl[3], double &t) {
-   const double w0 = pt[0] - S.p[0], w1 = pt[1] - S.p[1], w2 = pt[2] - S.p[2];
-   double c1 = 0.0;
-   c1 = c1 + w0 * S.v[0];
-   c1 = c1 + w1 * S.v[1];
-   c1 = c1 + w2 * S.v[2];
-   if (c1 < 0) {
-      cl[0] = S.p[0];
-      cl[1] = S.p[1];
-      cl[2] = S.p[2];
-      t = 0.0;
-   } else if (S.c2 <= c1) {
-      cl[0] = S.q[0];
-      cl[1] = S.q[1];
-      cl[2] = S.q[2];
-      t = 1.0;
-   } else {
-      const double b = c1 / S.c2;
-      cl[0] = S.p[0] + S.v[0] * b;
-      cl[1] = S.p[1] + S.v[1] * b;
-      cl[2] = S.p[2] + S.v[2] * b;
-      t = b;
-   }
-}
-
-// float(|cl - pt|^2) and float(r(t)^2) exactly as generator.cpp:327-328.
-__device__ __forceinline__ void exact_dist(const SegDev &S, const double pt[3],
-                                           double cl[3], float &dist_squ,
-                                           float &r_sqr) {
-   double t;
-   closest_point(S, pt, cl, t);
-   const double d0 = cl[0] - pt[0], d1 = cl[1] - pt[1], d2 = cl[2] - pt[2];
-   double l2 = 0.0;
-   l2 = l2 + d0 * d0;
-   l2 = l2 + d1 * d1;
-   l2 = l2 + d2 * d2;
-   dist_squ = (float)l2;
-   const double r = S.r0 * (1.0 - t) + S.r1 * t; // fiber.cpp:115-120
-   r_sqr = (float)(r * r);
-}
-
 __global__ void __launch_bounds__(128)
 tissue_keys(const SegDev *__restrict__ segs, int64_t n_segs,
             const LayerDev *__restrict__ layers, int64_t Y, int64_t Z,
             unsigned long long *__restrict__ keys,
-            unsigned *__restrict__ min_bundle) {
+            unsigned *__restrict__ min_bundle, unsigned long long *__restrict__ counters) {
+   unsigned long long n_slow = 0;
    for (int64_t s = blockIdx.x; s < n_segs; s += gridDim.x) {
       const SegDev &S = segs[s];
       const float f_ly = layers[S.bundle].f_ly_squ;
@@ -375,15 +383,20 @@ tissue_keys(const SegDev *__restrict__ segs, int64_t n_segs,
           (unsigned long long)(0xFFFFFFFFu - (unsigned)s);
       const float vfx = S.vf[0], vfy = S.vf[1], vfz = S.vf[2];
       const float c2f = S.c2f;
+      const bool fast_ok = S.pscale < 0x1p22f;
       for (int pl = threadIdx.x; pl < plane; pl += blockDim.x) {
          const int iy = pl / ez, iz = pl - (pl / ez) * ez;
          const int64_t y = S.lo[1] + iy, z = S.lo[2] + iz;
-         // FP32 prefilter in segment-local coordinates
-         const float wy = (float)(y - S.base[1]) + (0.5f - S.pf[1]);
-         const float wz = (float)(z - S.base[2]) + (0.5f - S.pf[2]);
+         // segment-local voxel centre, exact in float
+         const float ly = (float)(y - S.base[1]) + 0.5f;
+         const float lz = (float)(z - S.base[2]) + 0.5f;
+         // FP32 prefilter
+         const float wy = ly - S.pf[1];
+         const float wz = lz - S.pf[2];
          for (int ix = 0; ix < ex; ix++) {
             const int64_t x = S.lo[0] + ix;
-            const float wx = (float)(x - S.base[0]) + (0.5f - S.pf[0]);
+            const float lx = (float)(x - S.base[0]) + 0.5f;
+            const float wx = lx - S.pf[0];
             const float c1f = wx * vfx + wy * vfy + wz * vfz;
             const float w2 = wx * wx + wy * wy + wz * wz;
             float d2f;
@@ -398,13 +411,19 @@ tissue_keys(const SegDev *__restrict__ segs, int64_t n_segs,
             const float margin = 1e-4f + 3.8e-6f * (w2 + c2f);
             if (d2f - margin > S.thr_f)
                continue;
-            // exact reference arithmetic for the survivors
-            const double pt[3] = {(double)x + 0.5, (double)y + 0.5,
-                                  (double)z + 0.5};
-            double cl[3];
             float dist_squ, r_sqr;
-            exact_dist(S, pt, cl, dist_squ, r_sqr);
-            if (dist_squ > f_ly * r_sqr)
+            FastCand fc;
+            const float lpt[3] = {lx, ly, lz};
+            if (fast_ok && fast_candidate(S, lpt, fc)) {
+               dist_squ = fc.dist_squ;
+               r_sqr = fc.r_sqr;
+            } else { // exact reference arithmetic
+               const double pt[3] = {(double)x + 0.5, (double)y + 0.5, (double)z + 0.5};
+               double cl[3];
+               exact_dist(S, pt, cl, dist_squ, r_sqr);
+               n_slow++;
+            }
+            if (dist_squ > f_ly * r_sqr) // generator.cpp:329-331
                continue;
             const int64_t ind = (x * Y + y) * Z + z;
             const unsigned long long key =
@@ -415,16 +434,18 @@ tissue_keys(const SegDev *__restrict__ segs, int64_t n_segs,
          }
       }
    }
+   if (n_slow)
+      atomicAdd(&counters[9], n_slow);
 }
 
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 3)
 tissue_write(const unsigned long long *__restrict__ keys,
              const SegDev *__restrict__ segs,
              const LayerDev *__restrict__ layers, int max_layer, int64_t n_vox,
              int64_t Y, int64_t Z, int32_t *__restrict__ label,
              float *__restrict__ vec, const unsigned *__restrict__ min_bundle,
              unsigned long long *__restrict__ counters) {
-   unsigned long long n_overflow = 0, n_overlap = 0;
+   unsigned long long n_overflow = 0, n_overlap = 0, n_slow = 0;
    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_vox;
         i += (int64_t)gridDim.x * blockDim.x) {
       const unsigned long long key = keys[i];
@@ -445,10 +466,17 @@ tissue_write(const unsigned long long *__restrict__ keys,
       const int64_t xy = i / Z;
       const int64_t y = xy % Y;
       const int64_t x = xy / Y;
-      const double pt[3] = {(double)x + 0.5, (double)y + 0.5, (double)z + 0.5};
+      const float lpt[3] = {(float)(x - S.base[0]) + 0.5f, (float)(y - S.base[1]) + 0.5f,
+                            (float)(z - S.base[2]) + 0.5f};
+      FastCand fc;
+      bool fast = S.pscale < 0x1p22f && fast_candidate(S, lpt, fc);
+      float r_sqr = fc.r_sqr;
       double cl[3];
-      float d_chk, r_sqr;
-      exact_dist(S, pt, cl, d_chk, r_sqr);
+      const double pt[3] = {(double)x + 0.5, (double)y + 0.5, (double)z + 0.5};
+      if (!fast) {
+         float d_chk;
+         exact_dist(S, pt, cl, d_chk, r_sqr);
+      }
       // std::lower_bound(scale^2, double(dist_squ / r_sqr)) (generator.cpp:345-349)
       const double qv = (double)(dist_squ / r_sqr);
       int ly = 0;
@@ -457,23 +485,27 @@ tissue_write(const unsigned long long *__restrict__ keys,
       label[i] = ly + 1 + S.bundle * max_layer;
       if (min_bundle && min_bundle[i] < (unsigned)S.bundle)
          n_overlap++;
-      if (vec) {
-         double nv[3] = {0.0, 0.0, 0.0};
-         char m = 'b';
-         if (ly < L.n)
-            m = L.model[ly];
-         else
-            n_overflow++;
-         if (m == 'r') {
-            nv[0] = pt[0] - cl[0];
-            nv[1] = pt[1] - cl[1];
-            nv[2] = pt[2] - cl[2];
-         } else if (m == 'p') {
-            nv[0] = S.v[0];
-            nv[1] = S.v[1];
-            nv[2] = S.v[2];
-         }
-         if (m != 'b') { // vm::unit (vemath.hpp:390-402)
+      char m = 'b';
+      if (ly < L.n)
+         m = L.model[ly];
+      else
+         n_overflow++;
+      if (!vec)
+         continue;
+      float o[3] = {0.f, 0.f, 0.f};
+      if (m == 'p') {
+         o[0] = S.vp[0];
+         o[1] = S.vp[1];
+         o[2] = S.vp[2];
+      } else if (m == 'r') {
+         if (!(fast && fast_radial(S, fc, o))) {
+            if (fast) {
+               float d_chk, r_chk;
+               exact_dist(S, pt, cl, d_chk, r_chk);
+            }
+            n_slow++;
+            // vm::unit(point - closest) in the reference's double order
+            double nv[3] = {pt[0] - cl[0], pt[1] - cl[1], pt[2] - cl[2]};
             double n2 = 0.0;
             n2 = n2 + nv[0] * nv[0];
             n2 = n2 + nv[1] * nv[1];
@@ -484,18 +516,21 @@ tissue_write(const unsigned long long *__restrict__ keys,
                nv[1] = nv[1] * inv;
                nv[2] = nv[2] * inv;
             }
+            o[0] = (float)nv[0];
+            o[1] = (float)nv[1];
+            o[2] = (float)nv[2];
          }
-         vec[3 * i + 0] = (float)nv[0];
-         vec[3 * i + 1] = (float)nv[1];
-         vec[3 * i + 2] = (float)nv[2];
-      } else if (ly >= L.n) {
-         n_overflow++;
       }
+      vec[3 * i + 0] = o[0];
+      vec[3 * i + 1] = o[1];
+      vec[3 * i + 2] = o[2];
    }
    if (n_overlap)
       atomicAdd(&counters[0], n_overlap);
    if (n_overflow)
       atomicAdd(&counters[5], n_overflow);
+   if (n_slow)
+      atomicAdd(&counters[9], n_slow);
 }
 
 // ======================================================================
@@ -551,7 +586,7 @@ int run_tissue(const TissuePlan &p, int only_label, int32_t *d_label,
    if (!p.segs.empty()) {
       const int64_t n = (int64_t)p.segs.size();
       const unsigned grid = (unsigned)std::min<int64_t>(n, 1 << 30);
-      tissue_keys<<<grid, 128, 0, st>>>(segs, n, layers, p.Y, p.Z, keys, minb);
+      tissue_keys<<<grid, 128, 0, st>>>(segs, n, layers, p.Y, p.Z, keys, minb, counters);
       FPGB_CUDA_TRY(cudaGetLastError());
    }
    {

@@ -26,6 +26,17 @@ struct SegDev {
    int32_t lo[3];   // clipped box start (generator.cpp:304)
    int32_t ext[3];  // clipped box extent
    int32_t bundle;
+   // two-float copies (hi, lo) of the double inputs, for the fast path
+   float pl_hi[3], pl_lo[3]; // p - base
+   float v_hi[3], v_lo[3];   // v
+   float c2_hi, c2_lo;       // c2
+   float r0_hi, r0_lo;       // r0
+   float dr_hi, dr_lo;       // r1 - r0
+   float rsq0, rsq1;         // float(r^2) at t = 0 and t = 1 (exact)
+   float rsq_const;          // float(r^2) for every interior t when r0 == r1
+                             // and that rounding is certain; NaN otherwise
+   float pscale;             // max |coordinate| met by this segment's arithmetic
+   float vp[3];              // float(unit(q - p)): the 'p' layer vector (exact)
 };
 
 // Layers of one bundle, sorted by scale (fiber_bundle.cpp:83-86).

@@ -1,0 +1,154 @@
+// Exact (FP64) and two-float evaluation of one (segment, voxel) candidate of
+// the voxelizer.  Host+device: the kernels use it, and a host build checks
+// the two-float decisions against the FP64 replay.
+#pragma once
+
+#include <cmath>
+
+#include "ff.cuh"
+#include "tissue.cuh"
+
+namespace fpgb {
+
+// Closest point of `pt` on segment S and its parameter t, in the reference's
+// double operation order (generator.cpp:475-494).  -fmad=false keeps every
+// product and sum separately rounded.
+FPGB_HD void closest_point(const SegDev &S, const double pt[3],
+                                              double cl[3], double &t) {
+   const double w0 = pt[0] - S.p[0], w1 = pt[1] - S.p[1], w2 = pt[2] - S.p[2];
+   double c1 = 0.0;
+   c1 = c1 + w0 * S.v[0];
+   c1 = c1 + w1 * S.v[1];
+   c1 = c1 + w2 * S.v[2];
+   if (c1 < 0) {
+      cl[0] = S.p[0];
+      cl[1] = S.p[1];
+      cl[2] = S.p[2];
+      t = 0.0;
+   } else if (S.c2 <= c1) {
+      cl[0] = S.q[0];
+      cl[1] = S.q[1];
+      cl[2] = S.q[2];
+      t = 1.0;
+   } else {
+      const double b = c1 / S.c2;
+      cl[0] = S.p[0] + S.v[0] * b;
+      cl[1] = S.p[1] + S.v[1] * b;
+      cl[2] = S.p[2] + S.v[2] * b;
+      t = b;
+   }
+}
+
+// float(|cl - pt|^2) and float(r(t)^2) exactly as generator.cpp:327-328.
+FPGB_HD void exact_dist(const SegDev &S, const double pt[3],
+                                           double cl[3], float &dist_squ,
+                                           float &r_sqr) {
+   double t;
+   closest_point(S, pt, cl, t);
+   const double d0 = cl[0] - pt[0], d1 = cl[1] - pt[1], d2 = cl[2] - pt[2];
+   double l2 = 0.0;
+   l2 = l2 + d0 * d0;
+   l2 = l2 + d1 * d1;
+   l2 = l2 + d2 * d2;
+   dist_squ = (float)l2;
+   const double r = S.r0 * (1.0 - t) + S.r1 * t; // fiber.cpp:115-120
+   r_sqr = (float)(r * r);
+}
+
+// ----------------------------------------------------------------------
+// Two-float fast path.  For one (segment, voxel) pair it evaluates the
+// reference's double arithmetic in two-float precision (~2^-46 relative)
+// with an explicit bound E on |two-float value - value the reference's
+// double arithmetic produces| (rounding of the reference itself included,
+// generously).  A float result is accepted only when every real in
+// [value - E, value + E] rounds to the same float; branch decisions only
+// when the compared quantities differ by more than their bound.  Anything
+// else returns false and the caller replays the reference in FP64, so the
+// outcome is always the reference's, bit for bit.
+// ----------------------------------------------------------------------
+struct FastCand {
+   float dist_squ, r_sqr;
+   ff d[3];  // closest - point
+   float dn; // |d|
+   float m;  // magnitude scale of the terms that make up d
+};
+
+FPGB_HD bool fast_candidate(const SegDev &S, const float pt[3],
+                                               FastCand &c) {
+   ff w[3], v[3];
+#pragma unroll
+   for (int i = 0; i < 3; i++) {
+      w[i] = ff_add_f(ff{-S.pl_hi[i], -S.pl_lo[i]}, pt[i]); // point - p
+      v[i] = ff{S.v_hi[i], S.v_lo[i]};
+   }
+   const ff c1 = ff_dot3(w, v);
+   const ff c2{S.c2_hi, S.c2_lo};
+   const float wn = sqrtf(w[0].hi * w[0].hi + w[1].hi * w[1].hi + w[2].hi * w[2].hi);
+   const float vn = sqrtf(S.c2_hi);
+   const float ec = 0x1p-42f * (wn * vn + 1.f);
+   int branch;
+   if (c1.hi < -ec) {
+      branch = 0; // c1 < 0: closest = s0, t = 0 (generator.cpp:483-484)
+   } else {
+      const ff dq = ff_sub(c1, c2);
+      if (dq.hi > ec)
+         branch = 1; // c2 <= c1: closest = s1, t = 1 (:487-488)
+      else if (c1.hi > ec && dq.hi < -ec)
+         branch = 2; // interior: b = c1 / c2 (:490-493)
+      else
+         return false;
+   }
+   float bmag;
+   if (branch == 0) {
+      bmag = 0.f;
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+         c.d[i] = ff_neg(w[i]);
+      c.r_sqr = S.rsq0;
+   } else if (branch == 1) {
+      bmag = 1.f;
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+         c.d[i] = ff_sub(v[i], w[i]);
+      c.r_sqr = S.rsq1;
+   } else {
+      const ff b = ff_div(c1, c2);
+      bmag = b.hi;
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+         c.d[i] = ff_sub(ff_mul(v[i], b), w[i]);
+      if (!std::isnan(S.rsq_const)) {
+         c.r_sqr = S.rsq_const;
+      } else { // r = r0 (1 - t) + r1 t  (fiber.cpp:115-120)
+         const ff R = ff_add(ff{S.r0_hi, S.r0_lo}, ff_mul(ff{S.dr_hi, S.dr_lo}, b));
+         const ff R2 = ff_sqr(R);
+         const float er =
+             0x1p-40f * (R2.hi + fabsf(R.hi) * fabsf(S.dr_hi) * (bmag + wn / vn + 1.f));
+         if (!ff_round_unique(R2, er, c.r_sqr))
+            return false;
+      }
+   }
+   const ff D = ff_norm2(c.d);
+   c.dn = sqrtf(fmaxf(D.hi, 0.f));
+   c.m = wn + vn * bmag + 1.f;
+   const float ed = 0x1p-41f * c.m * (c.dn + 0x1p-20f * c.m) +
+                    0x1p-47f * S.pscale * (2.f * c.dn + 1.f);
+   return ff_round_unique(D, ed, c.dist_squ);
+}
+
+// float(unit(point - closest)) of the 'r' layer (generator.cpp:370-371)
+FPGB_HD bool fast_radial(const SegDev &S, const FastCand &c, float out[3]) {
+   if (!(c.dn > 0x1p-10f))
+      return false;
+   const ff n2 = ff_norm2(c.d);
+   const ff inv = ff_div(ff_from(-1.f), ff_sqrt(n2)); // nv = -d
+   const float ex = (0x1p-41f * c.m + 0x1p-47f * S.pscale) / c.dn + 0x1p-43f;
+#pragma unroll
+   for (int i = 0; i < 3; i++)
+      if (!ff_round_unique(ff_mul(c.d[i], inv), ex, out[i]))
+         return false;
+   return true;
+}
+
+
+} // namespace fpgb
