@@ -76,6 +76,8 @@ _SIGS = {
     "fpgb_generate_workspace_size": ([_P, _P], ctypes.c_size_t),
     "fpgb_generate_tissue_device": ([_P, _P, ctypes.c_int, _P, _P, _P, _I64, _P,
                                      _P, ctypes.c_size_t, _P, _P], ctypes.c_int),
+    "fpgb_generate_tissue_noalloc": ([_P, _P, ctypes.c_int, _P, _P, _P, _I64, _P, _P, _P],
+                                     ctypes.c_int),
     "fpgb_run_simulation": ([_P, _P, _P, _P, _P, _I64, _D, _D, _P, _P],
                             ctypes.c_int),
     "fpgb_run_simulation_device": ([_P, _P, _P, _P, _P, _I64, _D, _D, _P, _P, _P],

@@ -114,6 +114,26 @@ int fpgb_generate_tissue_device(const fpgb_volume *vol,
                                 size_t workspace_bytes, fpgb_warnings *warnings,
                                 void *stream);
 
+/* Voxelizer that allocates no device memory.  No counterpart in the
+ * reference (whose voxelizer runs on the host).  For callers that cannot call
+ * cudaMalloc (device memory owned by another allocator, or code that must not
+ * issue allocation calls): same inputs, outputs and results as
+ * fpgb_generate_tissue_device, but the scratch (keys, per-voxel bundle
+ * minima, segment/layer tables) lives in a fixed 64 MiB __device__ array of
+ * this library that every GPU loading it holds until exit.  Problems needing
+ * more scratch (about 8 bytes per voxel, 12 with several bundles, plus ~200
+ * bytes per fiber segment) are rejected with FPGB_EINVAL before any device
+ * work.  The first call on a device resolves the array's address with that
+ * device current; make it before any stream capture.  All calls on a device
+ * share the array: calls whose device work overlaps race and must be
+ * serialised. */
+int fpgb_generate_tissue_noalloc(const fpgb_volume *vol,
+                                 const fpgb_fibers *fibers, int only_label,
+                                 int32_t *d_label, float *d_vector,
+                                 double *props, int64_t props_cap,
+                                 int64_t *n_props, fpgb_warnings *warnings,
+                                 void *stream);
+
 /* ----------------------------------------------------------------------------
  * Ray march.  Replaces _Simulator.run_simulation
  * (simulator_module.cpp:61-93 -> PliSimulator::RunSimulation,

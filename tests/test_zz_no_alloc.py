@@ -1,0 +1,78 @@
+"""fpgb_generate_tissue_noalloc: the voxelizer entry point for callers that
+cannot allocate device memory (their GPU memory belongs to another
+allocator, or they must not issue allocation calls).  Its scratch is a fixed
+array inside the library; this file checks, through the C ABI, that it gives
+exactly the results of fpgb_generate_tissue_device on two calls in a row
+(the second reusing the scratch the first one left behind), and that a
+problem too large for the fixed scratch is refused before any device work.
+
+Named test_zz_* so that pytest collects it last."""
+
+import ctypes
+import warnings
+
+import numpy as np
+import pytest
+
+import cases
+from fastpli_gb300 import _native as N
+
+pytestmark = pytest.mark.gpu
+
+
+def _inputs(c):
+    flat = N.FlatFibers(c["bundles"], c["layers"])
+    vol = N.make_volume(c["dim"], c["origin"], c["voxel_size"])
+    return flat, vol
+
+
+def _run(torch, fn, c, extra_ws=False):
+    lib = N.load()
+    flat, vol = _inputs(c)
+    X, Y, Z = (int(v) for v in c["dim"])
+    label = torch.full((X, Y, Z), -7, dtype=torch.int32, device="cuda")
+    vector = torch.full((X, Y, Z, 3), 9.0, dtype=torch.float32, device="cuda")
+    props = np.zeros((flat.n_props, 2))
+    n_props = np.zeros(1, np.int64)
+    w = N.Warnings()
+    stream = torch.cuda.current_stream().cuda_stream
+    if fn == "noalloc":
+        rc = lib.fpgb_generate_tissue_noalloc(
+            N.byref(vol), N.byref(flat.struct), 0, N.ptr(label), N.ptr(vector), N.ptr(props),
+            flat.n_props, N.ptr(n_props), N.byref(w), stream)
+    else:
+        rc = lib.fpgb_generate_tissue_device(
+            N.byref(vol), N.byref(flat.struct), 0, N.ptr(label), N.ptr(vector), N.ptr(props),
+            flat.n_props, N.ptr(n_props), None, 0, N.byref(w), stream)
+    N.check(rc)
+    torch.cuda.synchronize()
+    return label.cpu().numpy(), vector.cpu().numpy(), props, w.as_dict()
+
+
+def test_noalloc_matches_device_entry_on_consecutive_calls(cuda):
+    torch = cuda
+    big = cases.synth_case(cases.crossing_small())   # two bundles, 307k voxels
+    small = cases.gen_cases()["edges"]               # different shape and layers
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        for c in (big, small, big):
+            ref = _run(torch, "device", c)
+            got = _run(torch, "noalloc", c)
+            assert np.array_equal(got[0], ref[0])
+            assert np.array_equal(got[1].view(np.uint32), ref[1].view(np.uint32))
+            assert np.array_equal(got[2], ref[2])
+            assert got[3] == ref[3]
+
+
+def test_noalloc_rejects_problems_beyond_its_scratch(cuda):
+    torch = cuda
+    c = dict(cases.gen_cases()["dimension"])
+    c["dim"] = np.array([512, 512, 64])  # 16.8 M voxels: 134 MB of keys
+    flat, vol = _inputs(c)
+    lib = N.load()
+    label = torch.empty(1, dtype=torch.int32, device="cuda")
+    rc = lib.fpgb_generate_tissue_noalloc(
+        N.byref(vol), N.byref(flat.struct), 1, N.ptr(label), None, None, 0, None, None,
+        torch.cuda.current_stream().cuda_stream)
+    assert rc == N.FPGB_EINVAL
+    assert b"scratch" in lib.fpgb_last_error()
