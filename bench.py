@@ -320,16 +320,209 @@ def run_gpu(args):
     return 0
 
 
+# ----------------------------------------------------------- tiles mode ---
+def run_tiles(args):
+    """Batched uneven tiles (``--workload tiles``): N tiles of the uneven-tile
+    mixture (xy 64-512, z 30-120 voxels at 0.2 um, 50-2000 fibers, per-tile
+    dn/mu), 5 tilts x 9 angles each, Slerp.  One step = the whole batch
+    (voxelize all tiles + march all pairs) replayed from a CUDA graph; the
+    plain per-call path (per tile: voxelize, then one march per tilt) is timed
+    on the same tiles for comparison."""
+    import torch
+    from fastpli_gb300 import autotune, synth
+    from fastpli_gb300.batch import TileBatch
+    from fastpli_gb300.simulation import _Generator, _Simulator
+    import fastpli_gb300
+    ws, rank, local = _dist_env()
+    torch.cuda.set_device(local)
+    fastpli_gb300.native_library()
+    from fastpli_gb300.shard import rank_units
+    tiles_all = synth.tiles(args.tiles)
+    mine = rank_units([t.n_voxels for t in tiles_all], ws, rank)
+    tiles = [tiles_all[i] for i in mine]
+    kw = tiles[0].setup_kwargs()
+    b = TileBatch(tiles, kw).allocate()
+    cfg, _, _ = autotune.tune(b, reps=1)
+    b.capture()
+    for _ in range(args.warmup):
+        b.replay()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        e0.record()
+        for _ in range(args.steps):
+            b.replay()
+        e1.record()
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    w = b.warnings()
+    steps = b.steps
+    vox = int(b.info.total_voxels)
+    # plain per-call path on the same tiles (device resident, no host copies)
+    sim = _Simulator()
+    sim.set_pli_setup(*_setup_args(tiles[0]))
+    gens = []
+    for t in tiles:
+        g = _Generator()
+        g.set_volume(t.dim, t.origin, t.voxel_size)
+        g.set_fiber_bundles(t.bundles, t.layers)
+        X, Y, Z = (int(v) for v in t.dim)
+        lab = torch.empty((X, Y, Z), dtype=torch.int32, device="cuda")
+        vec = torch.empty((X, Y, Z, 3), dtype=torch.float32, device="cuda")
+        img = torch.empty((X, Y, sim.n_rho), dtype=torch.float64, device="cuda")
+        wsp = torch.empty(g.workspace_size(), dtype=torch.uint8, device="cuda")
+        gens.append((g, t, lab, vec, img, wsp))
+
+    def plain():
+        for g, t, lab, vec, img, wsp in gens:
+            _, _, props, _ = g.run_generation_device(label=lab, vector=vec, workspace=wsp,
+                                                     sync_warnings=False)
+            for th, ph in t.tilts:
+                sim.run_simulation_device(t.dim, lab, vec, props, float(th), float(ph),
+                                          image=img, sync_warnings=False)
+    import warnings as _w
+    with _w.catch_warnings():
+        _w.simplefilter("ignore")
+        plain()
+        torch.cuda.synchronize()
+        p0 = time.perf_counter()
+        e0.record()
+        plain()
+        e1.record()
+        torch.cuda.synchronize()
+        plain_wall = time.perf_counter() - p0
+    plain_ms = e0.elapsed_time(e1)
+    ms = max_over_ranks_ms(ms, ws, local)
+    if rank == 0:
+        line = {"metric": "ray-voxel steps/s (uneven tile batch, voxelize + 5 tilts x 9 angles, "
+                          "Slerp)", "value": ws * steps / (ms * 1e-3), "unit": UNIT, "n_gpus": ws,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32", "data": "synthetic",
+                "config": {"workload": f"{len(tiles)} uneven tiles (64-512 xy, 30-120 z)",
+                           "voxels": vox, "pairs": int(b.info.n_pairs),
+                           "graph": "CUDA graph replay", "march_config": list(cfg),
+                           "l2": "inputs larger than L2"},
+                "tissue_voxels_per_s": None,
+                "plain_per_call": {"ms_per_batch_device": plain_ms,
+                                   "ms_per_batch_wall": plain_wall * 1e3,
+                                   "steps_per_s": steps / (plain_ms * 1e-3)},
+                "fp64_replays": w["fp64_replays"], "clocks": clocks.summary()}
+        print(json.dumps(line), flush=True)
+    b.close()
+    return 0
+
+
+# ----------------------------------------------------------- serve mode ---
+def run_serve(args):
+    """Serving (``--workload serve``): Poisson arrivals at each rate of
+    ``--rates``; every request is a tile of the uneven-tile mixture (a pool of
+    ``--pool`` seeded tiles) with 1 or 5 tilts (Bernoulli 1/2), Slerp, epa on
+    the device; HBM admission budget 150 GB.  The continuous-batching server
+    is compared with the plain per-call path serving the same arrival stream
+    one request at a time.  Reports p50/p99 arrival-to-result latency and
+    throughput per rate."""
+    import torch
+    import warnings as _w
+    from fastpli_gb300 import serving, synth
+    import fastpli_gb300
+    ws, rank, local = _dist_env()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    fastpli_gb300.native_library()
+    pool = [synth.tile(i) for i in range(args.pool)]
+    kw = pool[0].setup_kwargs()
+    rng = np.random.default_rng(5)
+
+    def stream_of(lam, n):
+        gaps = rng.exponential(1.0 / lam, n)
+        picks = rng.integers(0, len(pool), n)
+        five = rng.random(n) < 0.5
+        return np.cumsum(gaps), [(pool[i], synth.TILTS_5 if f else synth.TILTS_5[:1])
+                                 for i, f in zip(picks, five)]
+
+    def serve(server, arrivals, specs):
+        t0 = time.perf_counter()
+        reqs = []
+        with server:
+            for a, (tile, tilts) in zip(arrivals, specs):
+                d = t0 + a - time.perf_counter()
+                if d > 0:
+                    time.sleep(d)
+                reqs.append(server.submit(tile, tilts))
+            for r in reqs:
+                r.wait(600)
+        wall = time.perf_counter() - t0
+        st = serving.latency_stats(reqs)
+        st["throughput_rps"] = len(reqs) / wall
+        st["batches"] = server.batches
+        return st
+
+    with _w.catch_warnings():
+        _w.simplefilter("ignore")
+        # warm both paths (module load, autotune cache)
+        warm_a, warm_s = stream_of(1000.0, 8)
+        serve(serving.ForwardServer(kw, hbm_budget=150e9, max_tiles=32, n_slots=2), warm_a, warm_s)
+        serve(serving.ForwardServer(kw, hbm_budget=150e9, max_tiles=1, n_slots=1,
+                                    runner=serving.PlainRunner(kw)), warm_a, warm_s)
+        results = []
+        with ClockSampler(local) as clocks:
+            for lam in args.rates:
+                n = int(min(args.max_requests, max(40, lam * args.seconds)))
+                arrivals, specs = stream_of(lam, n)
+                batched = serve(serving.ForwardServer(kw, hbm_budget=150e9, max_tiles=32,
+                                                      n_slots=2), arrivals, specs)
+                plain = serve(serving.ForwardServer(kw, hbm_budget=150e9, max_tiles=1, n_slots=1,
+                                                    runner=serving.PlainRunner(kw)),
+                              arrivals, specs)
+                results.append({"rate_rps": lam, "requests": n, "batched": batched,
+                                "plain": plain})
+    best = max(r["batched"]["throughput_rps"] for r in results)
+    line = {"metric": "serving: requests/s and p50/p99 latency under Poisson load "
+                      "(uneven tiles, 1 or 5 tilts, Slerp, epa)",
+            "value": best, "unit": "requests/s", "n_gpus": 1, "steps": len(results),
+            "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"tile pool of {len(pool)} (64-512 xy, 30-120 z)",
+                       "hbm_budget_gb": 150, "max_tiles_per_batch": 32, "streams": 2},
+            "sweep": results, "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def max_over_ranks_ms(ms, ws, local):
+    if ws <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    if not dist.is_initialized():
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from fastpli_gb300.shard import max_over_ranks
+    return max_over_ranks(ms, dist, device=torch.device("cuda", local))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="crossing", choices=["crossing", "tiles", "serve"])
+    ap.add_argument("--rates", type=float, nargs="+", default=[10, 50, 200, 500],
+                    help="serve: Poisson arrival rates (requests/s)")
+    ap.add_argument("--seconds", type=float, default=4.0, help="serve: seconds per rate")
+    ap.add_argument("--max-requests", type=int, default=600, help="serve: cap per rate")
+    ap.add_argument("--pool", type=int, default=48, help="serve: distinct tiles")
+    ap.add_argument("--tiles", type=int, default=256, help="tiles of the tiles workload")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "tiles":
+        return run_tiles(args)
+    if args.workload == "serve":
+        return run_serve(args)
     return run_gpu(args)
 
 

@@ -1,0 +1,86 @@
+"""Launch-configuration tuner for the batched march.
+
+The persistent march kernel has two knobs that change speed but never
+results: resident CTAs per SM and work items (128-ray blocks) taken per queue
+grab.  ``tune(batch)`` times a small grid of both on the batch itself (CUDA
+events, after a warm-up run) and keeps the fastest; choices are cached in a
+JSON file keyed by device, interpolation mode and a coarse shape bucket
+(pairs, mean steps per ray), so a later batch of the same kind skips the
+search.  Cache path: ``$FPGB_AUTOTUNE_CACHE`` or ``fastpli_gb300/_lib/autotune.json``.
+"""
+
+import json
+import math
+import os
+import threading
+
+_LOCK = threading.Lock()
+_DEFAULT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "autotune.json")
+CTAS = (0, 4, 2)        # 0 = as many as fit
+GRABS = (1, 2, 4, 8)
+
+
+def cache_path():
+    return os.environ.get("FPGB_AUTOTUNE_CACHE", _DEFAULT)
+
+
+def _load():
+    try:
+        with open(cache_path()) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def _store(d):
+    p = cache_path()
+    os.makedirs(os.path.dirname(p), exist_ok=True)
+    tmp = p + ".tmp"
+    with open(tmp, "w") as f:
+        json.dump(d, f, indent=1, sort_keys=True)
+    os.replace(tmp, p)
+
+
+def key(batch):
+    import torch
+    name = torch.cuda.get_device_name()
+    interp = batch._setup.struct.interpolate
+    pairs = int(batch.info.n_pairs)
+    steps_per_ray = batch.steps / max(1, sum(
+        int(t.dim[0]) * int(t.dim[1]) * len(batch.pairs_of(i)) for i, t in enumerate(batch.tiles)))
+    return f"{name}|interp{interp}|pairs2^{int(math.log2(max(1, pairs)))}|z2^{int(math.log2(max(1, steps_per_ray)))}"
+
+
+def time_config(batch, ctas, grab, reps=3):
+    import torch
+    batch.run(ctas, grab)  # warm
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        batch.run(ctas, grab)
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def tune(batch, force=False, reps=3):
+    """Pick (ctas_per_sm, items_per_grab) for ``batch`` (already allocated);
+    sets ``batch.config`` and returns (config, ms, table)."""
+    k = key(batch)
+    with _LOCK:
+        cache = _load()
+    if not force and k in cache:
+        batch.config = tuple(cache[k]["config"])
+        return batch.config, cache[k]["ms"], None
+    table = {}
+    for c in CTAS:
+        for g in GRABS:
+            table[(c, g)] = time_config(batch, c, g, reps)
+    best = min(table, key=table.get)
+    batch.config = best
+    with _LOCK:
+        cache = _load()
+        cache[k] = {"config": list(best), "ms": table[best]}
+        _store(cache)
+    return best, table[best], table

@@ -1,0 +1,223 @@
+"""Batched forward model of many uneven tissue tiles (``include/fastpli_gb300_batch.h``).
+
+One ``TileBatch`` voxelizes every tile and marches every (tile, tilt) pair
+with one fixed launch sequence: the voxelizer key and write passes over all
+tiles, then a persistent march kernel that pulls blocks of rays from a queue
+ordered by cost.  The sequence allocates nothing and never synchronises, so it
+is captured once into a CUDA graph (``capture()``) and replayed
+(``replay()``).  Each tile's labels, vectors and images are bit-identical to
+the single-volume ``_Generator`` / ``_Simulator`` results.
+
+The launch configuration (resident CTAs per SM, work items per queue grab) is
+chosen by ``fastpli_gb300.autotune``.
+"""
+
+import ctypes
+
+import numpy as np
+
+from . import _native as N
+
+
+class BatchSizes(ctypes.Structure):
+    _fields_ = [("n_tiles", ctypes.c_int64), ("n_pairs", ctypes.c_int64),
+                ("n_items", ctypes.c_int64), ("n_segments", ctypes.c_int64),
+                ("total_voxels", ctypes.c_int64), ("steps", ctypes.c_int64),
+                ("arena_bytes", ctypes.c_size_t), ("workspace_bytes", ctypes.c_size_t)]
+
+
+_P = ctypes.c_void_p
+_SIGS = {
+    "fpgb_batch_create": ([ctypes.c_int64, _P, _P, _P, _P, _P, _P, ctypes.c_int, ctypes.c_int,
+                           _P], ctypes.c_int),
+    "fpgb_batch_info": ([_P, _P], ctypes.c_int),
+    "fpgb_batch_layout": ([_P, _P, _P, _P, _P, _P], ctypes.c_int),
+    "fpgb_batch_props": ([_P, ctypes.c_int64, _P, ctypes.c_int64], ctypes.c_int),
+    "fpgb_batch_upload": ([_P, _P, _P, _P], ctypes.c_int),
+    "fpgb_batch_run": ([_P, ctypes.c_int, ctypes.c_int, _P], ctypes.c_int),
+    "fpgb_batch_warnings": ([_P, _P, _P, _P], ctypes.c_int),
+    "fpgb_batch_destroy": ([_P], ctypes.c_int),
+}
+
+
+def lib():
+    L = N.load()
+    if not getattr(L, "_fpgb_batch_bound", False):
+        for name, (args, res) in _SIGS.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        L._fpgb_batch_bound = True
+    return L
+
+
+def exported_symbols():
+    return tuple(_SIGS)
+
+
+class TileBatch:
+    """Plan of a batch of tiles (host side).  ``tiles`` are objects with
+    ``dim``, ``origin``, ``voxel_size``, ``bundles``, ``layers``, ``tilts``
+    (e.g. ``fastpli_gb300.synth.Workload``); ``setup`` holds the keyword
+    arguments of ``_Simulator.set_pli_setup``."""
+
+    def __init__(self, tiles, setup, background_mu=None, epa=False):
+        L = lib()
+        self.tiles = list(tiles)
+        n = len(self.tiles)
+        if n == 0:
+            raise ValueError("empty batch")
+        self._flats = [N.FlatFibers(t.bundles, t.layers) for t in self.tiles]
+        self._vols = (N.Volume * n)(*[N.make_volume(t.dim, t.origin, t.voxel_size)
+                                      for t in self.tiles])
+        self._fibers = (N.Fibers * n)(*[f.struct for f in self._flats])
+        self._setup = N.SetupBlock(setup.get("step_size", 1.0), setup["light_intensity"],
+                                   setup["voxel_size"], setup["wavelength"],
+                                   setup.get("tissue_refrection", 1.0),
+                                   setup.get("interpolate", "Slerp"),
+                                   setup.get("untilt_sensor_view", True),
+                                   setup.get("flip_z", False), setup["filter_rotations"])
+        tilts = [np.asarray(t.tilts, np.float64).reshape(-1, 2) for t in self.tiles]
+        self.tilt_off = np.concatenate([[0], np.cumsum([len(t) for t in tilts])]).astype(np.int64)
+        self.tilts = np.ascontiguousarray(np.concatenate(tilts), np.float64)
+        self._bg = None if background_mu is None else np.ascontiguousarray(
+            np.broadcast_to(np.asarray(background_mu, np.float64), (n,)))
+        h = ctypes.c_void_p()
+        N.check(L.fpgb_batch_create(n, ctypes.addressof(self._vols), ctypes.addressof(self._fibers),
+                                    N.ptr(self._bg), N.byref(self._setup.struct),
+                                    N.ptr(self.tilt_off), N.ptr(self.tilts), int(bool(epa)), 0,
+                                    ctypes.byref(h)))
+        self._h = h
+        self.epa = bool(epa)
+        info = BatchSizes()
+        N.check(L.fpgb_batch_info(self._h, ctypes.byref(info)))
+        self.info = info
+        self.label_off = np.zeros(n, np.int64)
+        self.vector_off = np.zeros(n, np.int64)
+        self.n_props = np.zeros(n, np.int64)
+        self.image_off = np.zeros(info.n_pairs, np.int64)
+        self.epa_off = np.zeros(info.n_pairs, np.int64)
+        N.check(L.fpgb_batch_layout(self._h, N.ptr(self.label_off), N.ptr(self.vector_off),
+                                    N.ptr(self.image_off), N.ptr(self.epa_off),
+                                    N.ptr(self.n_props)))
+        self.pair_tile = np.repeat(np.arange(n), np.diff(self.tilt_off))
+        self.n_rho = self._setup.n_rho
+        self.arena = None
+        self.workspace = None
+        self._graph = None
+        self.config = (0, 0)
+
+    # ------------------------------------------------------------ sizes ---
+    @property
+    def steps(self):
+        return int(self.info.steps)
+
+    @property
+    def device_bytes(self):
+        return int(self.info.arena_bytes + self.info.workspace_bytes)
+
+    def props(self, t):
+        out = np.zeros((int(self.n_props[t]), 2))
+        N.check(lib().fpgb_batch_props(self._h, t, N.ptr(out), out.shape[0]))
+        return out
+
+    # ----------------------------------------------------------- device ---
+    def allocate(self, device="cuda", arena=None, workspace=None, stream=None):
+        """Bind device memory (torch uint8 tensors, allocated unless given) and
+        upload the tables."""
+        import torch
+        self.arena = arena if arena is not None else torch.empty(
+            int(self.info.arena_bytes), dtype=torch.uint8, device=device)
+        self.workspace = workspace if workspace is not None else torch.empty(
+            int(self.info.workspace_bytes), dtype=torch.uint8, device=device)
+        N.check(lib().fpgb_batch_upload(self._h, self.arena.data_ptr(),
+                                        self.workspace.data_ptr(), _stream(stream)))
+        return self
+
+    def run(self, ctas_per_sm=None, items_per_grab=None, stream=None):
+        c, g = self.config
+        c = c if ctas_per_sm is None else ctas_per_sm
+        g = g if items_per_grab is None else items_per_grab
+        N.check(lib().fpgb_batch_run(self._h, int(c), int(g), _stream(stream)))
+
+    def capture(self):
+        """Capture the batch's launch sequence into a CUDA graph."""
+        import torch
+        g = torch.cuda.CUDAGraph()
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            self.run(stream=s)  # warm module loading outside the capture
+        torch.cuda.current_stream().wait_stream(s)
+        torch.cuda.synchronize()
+        with torch.cuda.graph(g):
+            self.run()
+        self._graph = g
+        return g
+
+    def replay(self):
+        if self._graph is None:
+            self.capture()
+        self._graph.replay()
+
+    def warnings(self, stream=None):
+        w = N.Warnings()
+        replays = np.zeros(1, np.int64)
+        N.check(lib().fpgb_batch_warnings(self._h, N.byref(w), N.ptr(replays), _stream(stream)))
+        d = w.as_dict()
+        d["fp64_replays"] = int(replays[0])
+        return d
+
+    # ---------------------------------------------------------- results ---
+    def _view(self, off, count, dtype, shape):
+        import torch
+        nbytes = count * torch.empty((), dtype=dtype).element_size()
+        return self.arena[int(off): int(off) + nbytes].view(dtype).view(*shape)
+
+    def label(self, t):
+        import torch
+        X, Y, Z = (int(v) for v in self.tiles[t].dim)
+        return self._view(self.label_off[t], X * Y * Z, torch.int32, (X, Y, Z))
+
+    def vector(self, t):
+        import torch
+        X, Y, Z = (int(v) for v in self.tiles[t].dim)
+        return self._view(self.vector_off[t], 3 * X * Y * Z, torch.float32, (X, Y, Z, 3))
+
+    def image(self, p):
+        import torch
+        X, Y = (int(v) for v in self.tiles[self.pair_tile[p]].dim[:2])
+        return self._view(self.image_off[p], X * Y * self.n_rho, torch.float64,
+                          (X, Y, self.n_rho))
+
+    def epa_maps(self, p):
+        import torch
+        if not self.epa:
+            raise ValueError("batch planned without epa")
+        X, Y = (int(v) for v in self.tiles[self.pair_tile[p]].dim[:2])
+        e = self._view(self.epa_off[p], 3 * X * Y, torch.float64, (3, X, Y))
+        return e[0], e[1], e[2]
+
+    def pairs_of(self, t):
+        return list(range(int(self.tilt_off[t]), int(self.tilt_off[t + 1])))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().fpgb_batch_destroy(self._h)
+            self._h = None
+        self._graph = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _stream(stream):
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream

@@ -29,7 +29,7 @@ LIB_PATH = os.path.join(OUT_DIR, LIB_NAME)
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
           "-I", os.path.join(ROOT, "include")]
-PER_FILE = {"tissue.cu": ["-fmad=false"]}
+PER_FILE = {"tissue.cu": ["-fmad=false"], "batch_tissue.cu": ["-fmad=false"]}
 
 
 def _nvcc():
@@ -58,7 +58,7 @@ def _stale():
         return True
     t = os.path.getmtime(LIB_PATH)
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
-    deps.append(os.path.join(ROOT, "include", "fastpli_gb300.h"))
+    deps += [os.path.join(ROOT, "include", f) for f in os.listdir(os.path.join(ROOT, "include"))]
     deps.append(__file__)
     return any(os.path.getmtime(d) > t for d in deps)
 

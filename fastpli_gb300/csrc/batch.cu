@@ -1,0 +1,550 @@
+// Batched forward model: many tissue tiles of uneven size, each with its own
+// fibers, layers and tilt set, voxelized and marched by one fixed sequence of
+// launches that can be captured once in a CUDA graph and replayed.
+//
+//   batch_keys    the voxelizer key pass over the segments of ALL tiles (one
+//                 CTA per segment, as tissue_keys), each segment writing into
+//                 its tile's slice of one key arena;
+//   batch_write   label/vector for all tiles (grid.y = tile);
+//   batch_march   a persistent kernel: CTAs pull work items (tile-tilt pair,
+//                 block of rays) from an atomic counter in cost order until
+//                 the queue is empty, and march them with the same per-ray
+//                 code as the plain kernel (march_core.cuh).
+//
+// Every tile is computed with exactly the arithmetic of the single-volume
+// path, so a tile's results are bit-identical alone, in any batch, and
+// through fpgb_generate_tissue / fpgb_run_simulation.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "ff.cuh"
+#include "fpgb_common.cuh"
+#include "march_core.cuh"
+#include "raymarch.cuh"
+#include "tissue.cuh"
+#include "batch.cuh"
+
+namespace fpgb {
+
+
+struct BatchItem {
+   int32_t pair;
+   int32_t tilted;
+   int64_t ray_begin;
+   int32_t ray_count;
+   int32_t pad_;
+};
+
+struct fpgb_batch_impl {
+   fpgb_setup setup{};
+   std::vector<double> rotations;
+   std::vector<TissuePlan> tiles;
+   std::vector<TileDev> tile_dev;
+   std::vector<SegDev> segs;
+   std::vector<int32_t> seg_tile;
+   std::vector<LayerDev> layers;
+   std::vector<MarchPlan> pairs;
+   std::vector<int32_t> pair_tile;
+   std::vector<BatchItem> items;
+   // arena layout (bytes)
+   std::vector<size_t> label_off, vector_off, image_off, epa_off;
+   size_t arena_bytes = 0;
+   // workspace layout (bytes)
+   size_t ws_keys = 0, ws_minb = 0, ws_segs = 0, ws_segtile = 0, ws_layers = 0, ws_tiles = 0,
+          ws_prm = 0, ws_items = 0, ws_tables = 0, ws_counters = 0, ws_bytes = 0;
+   std::vector<size_t> table_off; // per pair: lut then ztab, relative to ws_tables
+   int64_t total_vox = 0, steps = 0;
+   bool any_multi_bundle = false;
+   int want_epa = 0;
+   // bound buffers
+   char *arena = nullptr, *ws = nullptr;
+   int rays_per_item = 0;
+   int64_t n_untilted = 0; // items [0, n_untilted) untilted, the rest tilted
+   int sms = 1;
+   int fit[2] = {1, 1}; // resident CTAs per SM of the untilted / tilted march
+};
+
+// ----------------------------------------------------------------------------
+// kernels
+// ----------------------------------------------------------------------------
+// Persistent march: every CTA loops taking the next item from the queue.
+// The loop ends when the counter passes n_items; there is no wait on any
+// other CTA or kernel.
+static_assert(sizeof(MarchParams) % 16 == 0, "MarchParams is copied as int4");
+constexpr int kBatchThreads = 128; // one work item = one CTA-width block of rays
+
+template <int MODE, bool TILT>
+__global__ void __launch_bounds__(128)
+batch_march(const MarchParams *__restrict__ prm, const BatchItem *__restrict__ items,
+            int64_t n_items, int chunk, unsigned long long *__restrict__ next,
+            unsigned long long *__restrict__ counters) {
+   __shared__ unsigned long long s_item;
+   // the item's parameter block, staged in shared memory (read like the
+   // plain kernel reads its by-value parameters)
+   __shared__ __align__(16) MarchParams sP;
+   int cur = -1;
+   for (;;) {
+      if (threadIdx.x == 0)
+         s_item = atomicAdd(next, (unsigned long long)chunk);
+      __syncthreads();
+      const unsigned long long it0 = s_item;
+      if (it0 >= (unsigned long long)n_items)
+         return;
+      const unsigned long long it1 = min(it0 + (unsigned long long)chunk,
+                                         (unsigned long long)n_items);
+      for (unsigned long long it = it0; it < it1; it++) {
+         const BatchItem w = items[it];
+         if (w.pair != cur) {
+            __syncthreads(); // everyone is done with the previous block
+            const int4 *src = reinterpret_cast<const int4 *>(prm + w.pair);
+            int4 *dst = reinterpret_cast<int4 *>(&sP);
+            for (int i = threadIdx.x; i < (int)(sizeof(MarchParams) / 16); i += blockDim.x)
+               dst[i] = src[i];
+            cur = w.pair;
+            __syncthreads();
+         }
+         for (int r = threadIdx.x; r < w.ray_count; r += blockDim.x)
+            march_one_ray<MODE, TILT>(sP, w.ray_begin + r, sP.label, sP.vec, sP.image,
+                                      sP.epa_t, sP.epa_d, sP.epa_r, counters);
+      }
+      __syncthreads(); // s_item is rewritten for the next chunk
+   }
+}
+
+template <int MODE, bool TILT>
+int batch_march_fit(int *fit) {
+   FPGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(fit, batch_march<MODE, TILT>,
+                                                              kBatchThreads, 0));
+   return FPGB_OK;
+}
+
+template <int MODE, bool TILT>
+int launch_batch_march(const MarchParams *prm, const BatchItem *items, int64_t n_items,
+                       unsigned long long *next, unsigned long long *counters, int sms, int fit,
+                       int ctas_per_sm, int chunk, cudaStream_t st) {
+   if (n_items <= 0)
+      return FPGB_OK;
+   const int per_sm = std::max(1, std::min(ctas_per_sm > 0 ? ctas_per_sm : fit, fit));
+   const int64_t grid = std::min<int64_t>((int64_t)sms * per_sm, (n_items + chunk - 1) / chunk);
+   batch_march<MODE, TILT><<<(unsigned)grid, kBatchThreads, 0, st>>>(prm, items, n_items, chunk,
+                                                                     next, counters);
+   FPGB_CUDA_TRY(cudaGetLastError());
+   return FPGB_OK;
+}
+
+// ----------------------------------------------------------------------------
+// host
+// ----------------------------------------------------------------------------
+namespace {
+
+int sm_count_now() {
+   int dev = 0, sms = 0;
+   cudaGetDevice(&dev);
+   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+   return sms > 0 ? sms : 1;
+}
+
+size_t take(size_t &cursor, size_t bytes) {
+   const size_t at = cursor;
+   cursor += align_up(std::max<size_t>(bytes, 1), 256);
+   return at;
+}
+
+int plan_batch(int64_t n_tiles, const fpgb_volume *vols, const fpgb_fibers *fibers,
+               const double *background_mu, const fpgb_setup *setup, const int64_t *tilt_off,
+               const double *tilts, int want_epa, int rays_per_item, fpgb_batch_impl *B) {
+   if (n_tiles <= 0 || !vols || !fibers || !tilt_off || !tilts) {
+      set_error("batch: empty or null input");
+      return FPGB_EINVAL;
+   }
+   if (n_tiles > 65535) { // the write pass puts tiles on grid.y
+      set_error("batch: at most 65535 tiles per batch, got %lld", (long long)n_tiles);
+      return FPGB_EINVAL;
+   }
+   FPGB_TRY(check_setup(setup));
+   B->setup = *setup;
+   B->rotations.assign(setup->filter_rotations, setup->filter_rotations + setup->n_rho);
+   B->setup.filter_rotations = B->rotations.data();
+   B->want_epa = want_epa;
+   (void)rays_per_item; // items are one CTA wide; fpgb_batch_run groups them
+   B->rays_per_item = kBatchThreads;
+   B->tiles.resize(n_tiles);
+   int64_t vox = 0;
+   for (int64_t t = 0; t < n_tiles; t++) {
+      TissuePlan &P = B->tiles[t];
+      FPGB_TRY(plan_tissue(&vols[t], &fibers[t], &P));
+      if (P.X * P.Y * P.Z >= (int64_t(1) << 32)) {
+         set_error("batch: tile %lld has 2^32 voxels or more", (long long)t);
+         return FPGB_EINVAL;
+      }
+      if (background_mu)
+         P.props[1] = background_mu[t];
+      TileDev T{};
+      T.vox_base = vox;
+      T.n_vox = P.X * P.Y * P.Z;
+      T.X = (int32_t)P.X;
+      T.Y = (int32_t)P.Y;
+      T.Z = (int32_t)P.Z;
+      T.max_layer = P.max_layer;
+      T.layer_base = (int32_t)B->layers.size();
+      B->tile_dev.push_back(T);
+      for (size_t s = 0; s < P.segs.size(); s++) {
+         B->segs.push_back(P.segs[s]);
+         B->seg_tile.push_back((int32_t)t);
+      }
+      for (int64_t b = 0; b < P.n_bundles; b++)
+         B->layers.push_back(P.layers[b]);
+      if (P.n_bundles == 0)
+         B->layers.push_back(LayerDev{});
+      B->any_multi_bundle |= P.n_bundles > 1;
+      vox += T.n_vox;
+   }
+   if (B->segs.size() > 0xFFFFFFF0ull) {
+      set_error("batch: too many segments");
+      return FPGB_EINVAL;
+   }
+   B->total_vox = vox;
+
+   // (tile, tilt) pairs and their march plans
+   for (int64_t t = 0; t < n_tiles; t++) {
+      const TissuePlan &P = B->tiles[t];
+      const int64_t dim[3] = {P.X, P.Y, P.Z};
+      if (tilt_off[t + 1] < tilt_off[t]) {
+         set_error("batch: tilt offsets must not decrease");
+         return FPGB_EINVAL;
+      }
+      for (int64_t k = tilt_off[t]; k < tilt_off[t + 1]; k++) {
+         MarchPlan mp;
+         FPGB_TRY(plan_march(&B->setup, dim, P.props.data(), (int64_t)P.props.size() / 2,
+                             tilts[2 * k], tilts[2 * k + 1], &mp));
+         mp.prm.tilted = (mp.prm.rotate || mp.prm.dx_fx != 0 || mp.prm.dy_fx != 0) ? 1 : 0;
+         B->steps += mp.steps;
+         B->pairs.push_back(std::move(mp));
+         B->pair_tile.push_back((int32_t)t);
+      }
+   }
+
+   // work items, most expensive first (rays x steps per ray)
+   for (size_t p = 0; p < B->pairs.size(); p++) {
+      const MarchParams &M = B->pairs[p].prm;
+      const int64_t rays = M.X * M.Y;
+      for (int64_t r0 = 0; r0 < rays; r0 += B->rays_per_item) {
+         BatchItem it{};
+         it.pair = (int32_t)p;
+         it.tilted = M.tilted;
+         it.ray_begin = r0;
+         it.ray_count = (int32_t)std::min<int64_t>(B->rays_per_item, rays - r0);
+         B->items.push_back(it);
+      }
+   }
+   // two queues (untilted items, then tilted items: separate kernels), each
+   // ordered by decreasing cost so that the dynamic queue balances well
+   std::stable_sort(B->items.begin(), B->items.end(), [&](const BatchItem &a, const BatchItem &b) {
+      if (a.tilted != b.tilted)
+         return a.tilted < b.tilted;
+      const int64_t ca = (int64_t)a.ray_count * B->pairs[a.pair].prm.n_z;
+      const int64_t cb = (int64_t)b.ray_count * B->pairs[b.pair].prm.n_z;
+      return ca > cb;
+   });
+   B->n_untilted = 0;
+   while (B->n_untilted < (int64_t)B->items.size() && !B->items[B->n_untilted].tilted)
+      B->n_untilted++;
+
+   // output arena: per tile label + vector, per pair image (+ epa)
+   size_t a = 0;
+   for (int64_t t = 0; t < n_tiles; t++) {
+      const int64_t n = B->tile_dev[t].n_vox;
+      B->label_off.push_back(take(a, sizeof(int32_t) * n));
+      B->vector_off.push_back(take(a, sizeof(float) * 3 * n));
+   }
+   for (size_t p = 0; p < B->pairs.size(); p++) {
+      const MarchParams &M = B->pairs[p].prm;
+      B->image_off.push_back(take(a, sizeof(double) * M.X * M.Y * M.n_rho));
+      B->epa_off.push_back(want_epa ? take(a, sizeof(double) * 3 * M.X * M.Y) : 0);
+   }
+   B->arena_bytes = a;
+
+   // workspace
+   size_t w = 0;
+   B->ws_keys = take(w, sizeof(unsigned long long) * vox);
+   B->ws_minb = B->any_multi_bundle ? take(w, sizeof(unsigned) * vox) : 0;
+   B->ws_segs = take(w, sizeof(SegDev) * B->segs.size());
+   B->ws_segtile = take(w, sizeof(int32_t) * B->seg_tile.size());
+   B->ws_layers = take(w, sizeof(LayerDev) * B->layers.size());
+   B->ws_tiles = take(w, sizeof(TileDev) * B->tile_dev.size() + 2 * sizeof(void *) * n_tiles);
+   B->ws_prm = take(w, sizeof(MarchParams) * B->pairs.size());
+   B->ws_items = take(w, sizeof(BatchItem) * B->items.size());
+   size_t tab = 0;
+   for (const MarchPlan &mp : B->pairs) {
+      B->table_off.push_back(tab);
+      tab += march_table_bytes(mp);
+   }
+   B->ws_tables = take(w, tab);
+   B->ws_counters = take(w, sizeof(unsigned long long) * (kCounterWords + 2));
+   B->ws_bytes = w;
+   return FPGB_OK;
+}
+
+int upload_batch(fpgb_batch_impl *B, void *arena, void *ws, cudaStream_t st) {
+   if (!arena || !ws || reinterpret_cast<uintptr_t>(arena) % 256 ||
+       reinterpret_cast<uintptr_t>(ws) % 256) {
+      set_error("batch: arena and workspace must be non-null and 256-byte aligned");
+      return FPGB_EINVAL;
+   }
+   B->arena = static_cast<char *>(arena);
+   B->ws = static_cast<char *>(ws);
+   char *W = B->ws;
+   FPGB_CUDA_TRY(cudaMemcpyAsync(W + B->ws_segs, B->segs.data(), sizeof(SegDev) * B->segs.size(),
+                                 cudaMemcpyHostToDevice, st));
+   FPGB_CUDA_TRY(cudaMemcpyAsync(W + B->ws_segtile, B->seg_tile.data(),
+                                 sizeof(int32_t) * B->seg_tile.size(), cudaMemcpyHostToDevice, st));
+   FPGB_CUDA_TRY(cudaMemcpyAsync(W + B->ws_layers, B->layers.data(),
+                                 sizeof(LayerDev) * B->layers.size(), cudaMemcpyHostToDevice, st));
+   // tile table followed by the per-tile label / vector pointer arrays
+   const size_t nt = B->tile_dev.size();
+   std::vector<char> tiles(sizeof(TileDev) * nt + 2 * sizeof(void *) * nt);
+   std::memcpy(tiles.data(), B->tile_dev.data(), sizeof(TileDev) * nt);
+   void **lp = reinterpret_cast<void **>(tiles.data() + sizeof(TileDev) * nt);
+   for (size_t t = 0; t < nt; t++) {
+      lp[t] = B->arena + B->label_off[t];
+      lp[nt + t] = B->arena + B->vector_off[t];
+   }
+   FPGB_CUDA_TRY(cudaMemcpyAsync(W + B->ws_tiles, tiles.data(), tiles.size(),
+                                 cudaMemcpyHostToDevice, st));
+   // per-pair parameter blocks with their tables and buffers bound
+   std::vector<MarchParams> prm(B->pairs.size());
+   for (size_t p = 0; p < B->pairs.size(); p++) {
+      const MarchPlan &mp = B->pairs[p];
+      MarchParams M = mp.prm;
+      char *tb = W + B->ws_tables + B->table_off[p];
+      FPGB_CUDA_TRY(cudaMemcpyAsync(tb, mp.lut.data(), sizeof(LabelOptics) * mp.lut.size(),
+                                    cudaMemcpyHostToDevice, st));
+      char *zt = tb + align_up(sizeof(LabelOptics) * mp.lut.size(), 256);
+      FPGB_CUDA_TRY(cudaMemcpyAsync(zt, mp.ztab.data(), sizeof(ZStep) * mp.ztab.size(),
+                                    cudaMemcpyHostToDevice, st));
+      M.lut = reinterpret_cast<const LabelOptics *>(tb);
+      M.ztab = reinterpret_cast<const ZStep *>(zt);
+      const int t = B->pair_tile[p];
+      M.label = reinterpret_cast<const int32_t *>(B->arena + B->label_off[t]);
+      M.vec = reinterpret_cast<const float *>(B->arena + B->vector_off[t]);
+      M.image = reinterpret_cast<double *>(B->arena + B->image_off[p]);
+      if (B->want_epa) {
+         double *e = reinterpret_cast<double *>(B->arena + B->epa_off[p]);
+         const int64_t n = M.X * M.Y;
+         M.epa_t = e;
+         M.epa_d = e + n;
+         M.epa_r = e + 2 * n;
+      } else {
+         M.epa_t = M.epa_d = M.epa_r = nullptr;
+      }
+      prm[p] = M;
+   }
+   FPGB_CUDA_TRY(cudaMemcpyAsync(W + B->ws_prm, prm.data(), sizeof(MarchParams) * prm.size(),
+                                 cudaMemcpyHostToDevice, st));
+   FPGB_CUDA_TRY(cudaMemcpyAsync(W + B->ws_items, B->items.data(),
+                                 sizeof(BatchItem) * B->items.size(), cudaMemcpyHostToDevice, st));
+   // host staging vectors must outlive the asynchronous copies
+   FPGB_CUDA_TRY(cudaStreamSynchronize(st));
+   // device queries happen here, so that fpgb_batch_run issues stream work only
+   B->sms = sm_count_now();
+   switch (B->setup.interpolate) {
+   case 0:
+      FPGB_TRY((batch_march_fit<0, false>(&B->fit[0])));
+      FPGB_TRY((batch_march_fit<0, true>(&B->fit[1])));
+      break;
+   case 1:
+      FPGB_TRY((batch_march_fit<1, false>(&B->fit[0])));
+      FPGB_TRY((batch_march_fit<1, true>(&B->fit[1])));
+      break;
+   default:
+      FPGB_TRY((batch_march_fit<2, false>(&B->fit[0])));
+      FPGB_TRY((batch_march_fit<2, true>(&B->fit[1])));
+      break;
+   }
+   return FPGB_OK;
+}
+
+
+// All device work of one batch: no allocation, no host synchronisation, so
+// a stream capture of this call is a complete graph of the batch.
+int run_batch(fpgb_batch_impl *B, int march_ctas_per_sm, int chunk, cudaStream_t st) {
+   if (!B->arena || !B->ws) {
+      set_error("batch: buffers not bound (call fpgb_batch_upload first)");
+      return FPGB_EINVAL;
+   }
+   char *W = B->ws;
+   auto *keys = reinterpret_cast<unsigned long long *>(W + B->ws_keys);
+   auto *minb = B->any_multi_bundle ? reinterpret_cast<unsigned *>(W + B->ws_minb) : nullptr;
+   auto *segs = reinterpret_cast<const SegDev *>(W + B->ws_segs);
+   auto *seg_tile = reinterpret_cast<const int32_t *>(W + B->ws_segtile);
+   auto *layers = reinterpret_cast<const LayerDev *>(W + B->ws_layers);
+   auto *tiles = reinterpret_cast<const TileDev *>(W + B->ws_tiles);
+   const size_t nt = B->tile_dev.size();
+   auto *lptr = reinterpret_cast<int32_t *const *>(W + B->ws_tiles + sizeof(TileDev) * nt);
+   auto *vptr = reinterpret_cast<float *const *>(W + B->ws_tiles + sizeof(TileDev) * nt +
+                                                 sizeof(void *) * nt);
+   auto *prm = reinterpret_cast<const MarchParams *>(W + B->ws_prm);
+   auto *items = reinterpret_cast<const BatchItem *>(W + B->ws_items);
+   auto *counters = reinterpret_cast<unsigned long long *>(W + B->ws_counters);
+   unsigned long long *next = counters + kCounterWords;
+
+   FPGB_CUDA_TRY(cudaMemsetAsync(keys, 0xFF, sizeof(unsigned long long) * B->total_vox, st));
+   if (minb)
+      FPGB_CUDA_TRY(cudaMemsetAsync(minb, 0xFF, sizeof(unsigned) * B->total_vox, st));
+   FPGB_CUDA_TRY(cudaMemsetAsync(counters, 0, sizeof(unsigned long long) * (kCounterWords + 2),
+                                 st));
+   const int sms = B->sms;
+   {
+      int64_t maxv = 0;
+      for (const TileDev &T : B->tile_dev)
+         maxv = std::max(maxv, T.n_vox);
+      FPGB_TRY(launch_batch_tissue(segs, seg_tile, (int64_t)B->segs.size(), tiles, (int64_t)nt,
+                                   maxv, layers, keys, minb, lptr, vptr, counters, sms, st));
+   }
+   const int64_t n0 = B->n_untilted, n1 = (int64_t)B->items.size() - B->n_untilted;
+   const int ch = chunk > 0 ? chunk : 4;
+#define FPGB_BATCH_MARCH(M)                                                                    \
+   FPGB_TRY((launch_batch_march<M, false>(prm, items, n0, next, counters, B->sms, B->fit[0],   \
+                                          march_ctas_per_sm, ch, st)));                        \
+   FPGB_TRY((launch_batch_march<M, true>(prm, items + n0, n1, next + 1, counters, B->sms,      \
+                                         B->fit[1], march_ctas_per_sm, ch, st)))
+   switch (B->setup.interpolate) {
+   case 0: FPGB_BATCH_MARCH(0); break;
+   case 1: FPGB_BATCH_MARCH(1); break;
+   default: FPGB_BATCH_MARCH(2); break;
+   }
+#undef FPGB_BATCH_MARCH
+   return FPGB_OK;
+}
+
+} // namespace
+} // namespace fpgb
+
+using namespace fpgb;
+
+struct fpgb_batch : fpgb_batch_impl {};
+
+extern "C" {
+
+int fpgb_batch_create(int64_t n_tiles, const fpgb_volume *vols, const fpgb_fibers *fibers,
+                      const double *background_mu, const fpgb_setup *setup,
+                      const int64_t *tilt_off, const double *tilts, int want_epa,
+                      int rays_per_item, fpgb_batch **out) {
+   if (!out) {
+      set_error("batch: null output handle");
+      return FPGB_EINVAL;
+   }
+   *out = nullptr;
+   std::unique_ptr<fpgb_batch> B(new fpgb_batch());
+   FPGB_TRY(plan_batch(n_tiles, vols, fibers, background_mu, setup, tilt_off, tilts, want_epa,
+                       rays_per_item, B.get()));
+   *out = B.release();
+   return FPGB_OK;
+}
+
+int fpgb_batch_info(const fpgb_batch *b, fpgb_batch_sizes *info) {
+   if (!b || !info) {
+      set_error("batch: null argument");
+      return FPGB_EINVAL;
+   }
+   info->n_tiles = (int64_t)b->tiles.size();
+   info->n_pairs = (int64_t)b->pairs.size();
+   info->n_items = (int64_t)b->items.size();
+   info->n_segments = (int64_t)b->segs.size();
+   info->total_voxels = b->total_vox;
+   info->steps = b->steps;
+   info->arena_bytes = b->arena_bytes;
+   info->workspace_bytes = b->ws_bytes;
+   return FPGB_OK;
+}
+
+int fpgb_batch_layout(const fpgb_batch *b, int64_t *label_off, int64_t *vector_off,
+                      int64_t *image_off, int64_t *epa_off, int64_t *n_props) {
+   if (!b) {
+      set_error("batch: null handle");
+      return FPGB_EINVAL;
+   }
+   for (size_t t = 0; t < b->tiles.size(); t++) {
+      if (label_off)
+         label_off[t] = (int64_t)b->label_off[t];
+      if (vector_off)
+         vector_off[t] = (int64_t)b->vector_off[t];
+      if (n_props)
+         n_props[t] = (int64_t)b->tiles[t].props.size() / 2;
+   }
+   for (size_t p = 0; p < b->pairs.size(); p++) {
+      if (image_off)
+         image_off[p] = (int64_t)b->image_off[p];
+      if (epa_off)
+         epa_off[p] = b->want_epa ? (int64_t)b->epa_off[p] : -1;
+   }
+   return FPGB_OK;
+}
+
+int fpgb_batch_props(const fpgb_batch *b, int64_t tile, double *props, int64_t props_cap) {
+   if (!b || tile < 0 || tile >= (int64_t)b->tiles.size() || !props) {
+      set_error("batch: bad tile or buffer");
+      return FPGB_EINVAL;
+   }
+   const std::vector<double> &p = b->tiles[tile].props;
+   if (props_cap < (int64_t)p.size() / 2) {
+      set_error("batch: props_cap too small");
+      return FPGB_EINVAL;
+   }
+   std::memcpy(props, p.data(), sizeof(double) * p.size());
+   return FPGB_OK;
+}
+
+int fpgb_batch_upload(fpgb_batch *b, void *d_arena, void *d_workspace, void *stream) {
+   if (!b) {
+      set_error("batch: null handle");
+      return FPGB_EINVAL;
+   }
+   return upload_batch(b, d_arena, d_workspace, as_stream(stream));
+}
+
+int fpgb_batch_run(fpgb_batch *b, int march_ctas_per_sm, int items_per_grab, void *stream) {
+   if (!b) {
+      set_error("batch: null handle");
+      return FPGB_EINVAL;
+   }
+   return run_batch(b, march_ctas_per_sm, items_per_grab, as_stream(stream));
+}
+
+int fpgb_batch_warnings(const fpgb_batch *b, fpgb_warnings *w, int64_t *fp64_replays,
+                        void *stream) {
+   if (!b || !b->ws) {
+      set_error("batch: buffers not bound");
+      return FPGB_EINVAL;
+   }
+   cudaStream_t st = as_stream(stream);
+   unsigned long long h[kCounterWords];
+   FPGB_CUDA_TRY(cudaMemcpyAsync(h, b->ws + b->ws_counters, sizeof h, cudaMemcpyDeviceToHost, st));
+   FPGB_CUDA_TRY(cudaStreamSynchronize(st));
+   if (h[6] & kStatusLabelRange) {
+      set_error("batch: label out of range");
+      return FPGB_EINVAL;
+   }
+   if (w) {
+      warnings_from_counters(reinterpret_cast<const long long *>(h), w);
+      w->overlap = w->overlap > 0 ? 1 : 0;
+      int64_t sp = 0;
+      for (const TissuePlan &t : b->tiles)
+         sp += t.single_point;
+      w->single_point = sp;
+   }
+   if (fp64_replays)
+      *fp64_replays = (int64_t)h[9];
+   return FPGB_OK;
+}
+
+int fpgb_batch_destroy(fpgb_batch *b) {
+   delete b;
+   return FPGB_OK;
+}
+
+} // extern "C"

@@ -10,6 +10,7 @@
 #include <string>
 
 #include "../../include/fastpli_gb300.h"
+#include "../../include/fastpli_gb300_batch.h"
 
 namespace fpgb {
 

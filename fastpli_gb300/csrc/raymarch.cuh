@@ -46,6 +46,13 @@ struct MarchParams {
    float epa_sin[kMaxRho], epa_cos[kMaxRho]; // sin/cos(2*pi*i/n) of epa.py:29
    const LabelOptics *lut;
    const ZStep *ztab;
+   // buffers of one (tile, tilt) pair of the batched path (unused by the
+   // plain kernel, which takes them as launch arguments)
+   const int32_t *label;
+   const float *vec;
+   double *image, *epa_t, *epa_d, *epa_r;
+   int32_t tilted; // x/y advance or the axis rotates
+   int32_t pad_;
 };
 
 struct MarchPlan {
@@ -58,4 +65,12 @@ struct MarchPlan {
 int plan_march(const fpgb_setup *setup, const int64_t *dim, const double *props,
                int64_t n_props, double theta, double phi, MarchPlan *plan);
 
+} // namespace fpgb
+
+namespace fpgb {
+int check_setup(const fpgb_setup *s);
+size_t march_table_bytes(const MarchPlan &mp);
+int init_counters(unsigned long long *d_counters, cudaStream_t st);
+int finish_counters(const unsigned long long *d_counters, int64_t n_props, bool checked_all,
+                    fpgb_warnings *w, cudaStream_t st);
 } // namespace fpgb

@@ -216,6 +216,12 @@ int plan_tissue(const fpgb_volume *vol, const fpgb_fibers *fb, TissuePlan *plan)
          L.dn[i] = fb->layer_dn[l];
          L.mu[i] = fb->layer_mu[l];
       }
+      for (int i = 0; i < n; i++) {
+         float f = (float)L.scale_sq[i];
+         if ((double)f > L.scale_sq[i])
+            f = std::nextafter(f, -INFINITY);
+         L.sq_fdown[i] = f;
+      }
       if (n > 0) {
          L.f_ly_squ = (float)L.scale_sq[n - 1];
          L.sqrt_last = std::sqrt(L.scale_sq[n - 1]);
@@ -386,15 +392,18 @@ tissue_keys(const SegDev *__restrict__ segs, int64_t n_segs,
       const bool fast_ok = S.pscale < 0x1p22f;
       for (int pl = threadIdx.x; pl < plane; pl += blockDim.x) {
          const int iy = pl / ez, iz = pl - (pl / ez) * ez;
-         const int64_t y = S.lo[1] + iy, z = S.lo[2] + iz;
+         const int y = S.lo[1] + iy, z = S.lo[2] + iz;
          // segment-local voxel centre, exact in float
          const float ly = (float)(y - S.base[1]) + 0.5f;
          const float lz = (float)(z - S.base[2]) + 0.5f;
          // FP32 prefilter
          const float wy = ly - S.pf[1];
          const float wz = lz - S.pf[2];
+         FastRow row;
+         if (fast_ok)
+            fast_row(S, ly, lz, row);
          for (int ix = 0; ix < ex; ix++) {
-            const int64_t x = S.lo[0] + ix;
+            const int x = S.lo[0] + ix;
             const float lx = (float)(x - S.base[0]) + 0.5f;
             const float wx = lx - S.pf[0];
             const float c1f = wx * vfx + wy * vfy + wz * vfz;
@@ -413,8 +422,7 @@ tissue_keys(const SegDev *__restrict__ segs, int64_t n_segs,
                continue;
             float dist_squ, r_sqr;
             FastCand fc;
-            const float lpt[3] = {lx, ly, lz};
-            if (fast_ok && fast_candidate(S, lpt, fc)) {
+            if (fast_ok && fast_candidate_row(S, lx, row, fc)) {
                dist_squ = fc.dist_squ;
                r_sqr = fc.r_sqr;
             } else { // exact reference arithmetic
@@ -425,7 +433,7 @@ tissue_keys(const SegDev *__restrict__ segs, int64_t n_segs,
             }
             if (dist_squ > f_ly * r_sqr) // generator.cpp:329-331
                continue;
-            const int64_t ind = (x * Y + y) * Z + z;
+            const int64_t ind = ((int64_t)x * Y + y) * Z + z;
             const unsigned long long key =
                 ((unsigned long long)__float_as_uint(dist_squ) << 32) | inv_idx;
             atomicMin(&keys[ind], key);
@@ -446,6 +454,7 @@ tissue_write(const unsigned long long *__restrict__ keys,
              float *__restrict__ vec, const unsigned *__restrict__ min_bundle,
              unsigned long long *__restrict__ counters) {
    unsigned long long n_overflow = 0, n_overlap = 0, n_slow = 0;
+   const bool small_index = n_vox < (int64_t(1) << 32);
    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_vox;
         i += (int64_t)gridDim.x * blockDim.x) {
       const unsigned long long key = keys[i];
@@ -462,25 +471,34 @@ tissue_write(const unsigned long long *__restrict__ keys,
       const float dist_squ = __uint_as_float((unsigned)(key >> 32));
       const SegDev &S = segs[seg];
       const LayerDev &L = layers[S.bundle];
-      const int64_t z = i % Z;
-      const int64_t xy = i / Z;
-      const int64_t y = xy % Y;
-      const int64_t x = xy / Y;
+      int x, y, z;
+      if (small_index) {
+         const unsigned ii = (unsigned)i, zz = (unsigned)Z, yy = (unsigned)Y;
+         const unsigned xy = ii / zz;
+         z = (int)(ii - xy * zz);
+         x = (int)(xy / yy);
+         y = (int)(xy - (unsigned)x * yy);
+      } else {
+         z = (int)(i % Z);
+         const int64_t xy = i / Z;
+         y = (int)(xy % Y);
+         x = (int)(xy / Y);
+      }
       const float lpt[3] = {(float)(x - S.base[0]) + 0.5f, (float)(y - S.base[1]) + 0.5f,
                             (float)(z - S.base[2]) + 0.5f};
       FastCand fc;
       bool fast = S.pscale < 0x1p22f && fast_candidate(S, lpt, fc);
       float r_sqr = fc.r_sqr;
       double cl[3];
-      const double pt[3] = {(double)x + 0.5, (double)y + 0.5, (double)z + 0.5};
       if (!fast) {
+         const double pt[3] = {(double)x + 0.5, (double)y + 0.5, (double)z + 0.5};
          float d_chk;
          exact_dist(S, pt, cl, d_chk, r_sqr);
       }
       // std::lower_bound(scale^2, double(dist_squ / r_sqr)) (generator.cpp:345-349)
-      const double qv = (double)(dist_squ / r_sqr);
+      const float qv = dist_squ / r_sqr;
       int ly = 0;
-      while (ly < L.n && L.scale_sq[ly] < qv)
+      while (ly < L.n && qv > L.sq_fdown[ly])
          ly++;
       label[i] = ly + 1 + S.bundle * max_layer;
       if (min_bundle && min_bundle[i] < (unsigned)S.bundle)
@@ -499,6 +517,7 @@ tissue_write(const unsigned long long *__restrict__ keys,
          o[2] = S.vp[2];
       } else if (m == 'r') {
          if (!(fast && fast_radial(S, fc, o))) {
+            const double pt[3] = {(double)x + 0.5, (double)y + 0.5, (double)z + 0.5};
             if (fast) {
                float d_chk, r_chk;
                exact_dist(S, pt, cl, d_chk, r_chk);

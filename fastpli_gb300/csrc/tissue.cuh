@@ -45,6 +45,9 @@ struct LayerDev {
    float f_ly_squ = 0.f; // float(scale^2 of the outermost layer)
    double sqrt_last = 0.0;
    double scale_sq[kMaxLayers] = {};
+   // largest float <= scale_sq[l]: for a float q, (double)q > scale_sq[l]
+   // exactly when q > sq_fdown[l], so the layer search needs no FP64
+   float sq_fdown[kMaxLayers] = {};
    double dn[kMaxLayers] = {};
    double mu[kMaxLayers] = {};
    char model[kMaxLayers] = {};

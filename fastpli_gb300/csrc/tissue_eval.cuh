@@ -73,17 +73,30 @@ struct FastCand {
    float m;  // magnitude scale of the terms that make up d
 };
 
-FPGB_HD bool fast_candidate(const SegDev &S, const float pt[3],
-                                               FastCand &c) {
+// Per-(y, z) row terms of the candidate evaluation (hoisted out of the x loop).
+struct FastRow {
+   ff wy, wz, c1yz; // point - p along y and z, and their part of dot(w, v)
+   float wyz2;      // float estimate of wy^2 + wz^2
+};
+
+FPGB_HD void fast_row(const SegDev &S, float ly, float lz, FastRow &r) {
+   r.wy = ff_add_f(ff{-S.pl_hi[1], -S.pl_lo[1]}, ly);
+   r.wz = ff_add_f(ff{-S.pl_hi[2], -S.pl_lo[2]}, lz);
+   r.c1yz = ff_add(ff_mul(r.wy, ff{S.v_hi[1], S.v_lo[1]}), ff_mul(r.wz, ff{S.v_hi[2], S.v_lo[2]}));
+   r.wyz2 = r.wy.hi * r.wy.hi + r.wz.hi * r.wz.hi;
+}
+
+FPGB_HD bool fast_candidate_row(const SegDev &S, float lx, const FastRow &row, FastCand &c) {
    ff w[3], v[3];
+   w[0] = ff_add_f(ff{-S.pl_hi[0], -S.pl_lo[0]}, lx); // point - p
+   w[1] = row.wy;
+   w[2] = row.wz;
 #pragma unroll
-   for (int i = 0; i < 3; i++) {
-      w[i] = ff_add_f(ff{-S.pl_hi[i], -S.pl_lo[i]}, pt[i]); // point - p
+   for (int i = 0; i < 3; i++)
       v[i] = ff{S.v_hi[i], S.v_lo[i]};
-   }
-   const ff c1 = ff_dot3(w, v);
+   const ff c1 = ff_add(ff_mul(w[0], v[0]), row.c1yz);
+   const float wn = sqrtf(w[0].hi * w[0].hi + row.wyz2);
    const ff c2{S.c2_hi, S.c2_lo};
-   const float wn = sqrtf(w[0].hi * w[0].hi + w[1].hi * w[1].hi + w[2].hi * w[2].hi);
    const float vn = sqrtf(S.c2_hi);
    const float ec = 0x1p-42f * (wn * vn + 1.f);
    int branch;
@@ -134,6 +147,12 @@ FPGB_HD bool fast_candidate(const SegDev &S, const float pt[3],
    const float ed = 0x1p-41f * c.m * (c.dn + 0x1p-20f * c.m) +
                     0x1p-47f * S.pscale * (2.f * c.dn + 1.f);
    return ff_round_unique(D, ed, c.dist_squ);
+}
+
+FPGB_HD bool fast_candidate(const SegDev &S, const float pt[3], FastCand &c) {
+   FastRow row;
+   fast_row(S, pt[1], pt[2], row);
+   return fast_candidate_row(S, pt[0], row, c);
 }
 
 // float(unit(point - closest)) of the 'r' layer (generator.cpp:370-371)

@@ -1,0 +1,111 @@
+"""Batched uneven tiles: host planning on CPU; on the GPU every tile's labels,
+vectors and images must be bit-identical to the single-volume entry points,
+and a CUDA-graph replay must reproduce the first run."""
+
+import warnings
+
+import numpy as np
+import pytest
+
+import cases
+from fastpli_gb300 import batch as B
+from fastpli_gb300 import synth
+from fastpli_gb300.simulation import _Generator, _Simulator
+
+
+def small_tiles(n=5, seed_base=500):
+    out = []
+    for i in range(n):
+        t = synth.tile(i, seed_base=seed_base, n_fibers=12 + 5 * i)
+        # shrink to test size, keep uneven shapes (odd z sizes included)
+        rng = np.random.default_rng(seed_base + i)
+        X, Y = (int(v) for v in rng.integers(17, 57, 2))
+        Z = int(rng.integers(7, 31))
+        t.dim = np.array([X, Y, Z])
+        out.append(t)
+    return out
+
+
+def test_plan_is_host_only_and_consistent():
+    tiles = small_tiles()
+    b = B.TileBatch(tiles, dict(tiles[0].setup_kwargs()), epa=True)
+    n = len(tiles)
+    assert b.info.n_tiles == n and b.info.n_pairs == sum(len(t.tilts) for t in tiles)
+    assert b.info.total_voxels == sum(int(np.prod(t.dim)) for t in tiles)
+    offs = sorted(list(b.label_off) + list(b.vector_off) + list(b.image_off) + list(b.epa_off))
+    assert all(o % 256 == 0 for o in offs)
+    assert len(set(offs)) == len(offs)  # no two buffers share an offset
+    assert b.info.arena_bytes > max(offs)
+    sim = _Simulator()
+    kw = tiles[0].setup_kwargs()
+    sim.set_pli_setup(kw["step_size"], kw["light_intensity"], kw["voxel_size"], kw["wavelength"],
+                      kw["tissue_refrection"], kw["interpolate"], kw["untilt_sensor_view"],
+                      kw["flip_z"], kw["filter_rotations"])
+    steps = sum(sim.count_steps(t.dim, th, ph) for t in tiles for th, ph in t.tilts)
+    assert b.steps == steps
+    assert np.array_equal(b.props(2)[1:], B.TileBatch([tiles[2]], kw).props(0)[1:])
+    b.close()
+
+
+def test_symbols_exported():
+    L = B.lib()
+    for name in B.exported_symbols():
+        assert hasattr(L, name)
+
+
+@pytest.mark.gpu
+def test_batch_bit_identical_to_single_volume_path(cuda):
+    torch = cuda
+    tiles = small_tiles()
+    kw = tiles[0].setup_kwargs()
+    b = B.TileBatch(tiles, kw, epa=True).allocate()
+    b.run()
+    torch.cuda.synchronize()
+    w = b.warnings()
+    sim = _Simulator()
+    sim.set_pli_setup(kw["step_size"], kw["light_intensity"], kw["voxel_size"], kw["wavelength"],
+                      kw["tissue_refrection"], kw["interpolate"], kw["untilt_sensor_view"],
+                      kw["flip_z"], kw["filter_rotations"])
+    for t, tile in enumerate(tiles):
+        g = _Generator()
+        g.set_volume(tile.dim, tile.origin, tile.voxel_size)
+        g.set_fiber_bundles(tile.bundles, tile.layers)
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            lab, vec, props = g.run_generation()
+        assert np.array_equal(b.label(t).cpu().numpy(), lab), f"tile {t} labels"
+        assert np.array_equal(b.vector(t).cpu().numpy().view(np.uint32), vec.view(np.uint32))
+        for p in b.pairs_of(t):
+            th, ph = b.tilts[p]
+            ref = sim.run_simulation(tile.dim, lab, vec, props, th, ph)
+            assert np.array_equal(b.image(p).cpu().numpy(), ref), f"tile {t} pair {p}"
+    assert w["fp64_replays"] >= 0
+    # a CUDA-graph replay reproduces the run exactly
+    before = [b.image(p).clone() for p in range(int(b.info.n_pairs))]
+    b.arena.zero_()
+    b.replay()
+    torch.cuda.synchronize()
+    for p in range(int(b.info.n_pairs)):
+        assert torch.equal(b.image(p), before[p])
+    b.close()
+
+
+@pytest.mark.gpu
+def test_autotune_picks_a_config_and_results_do_not_change(cuda, tmp_path, monkeypatch):
+    torch = cuda
+    from fastpli_gb300 import autotune
+    monkeypatch.setenv("FPGB_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    tiles = small_tiles(3, seed_base=700)
+    b = B.TileBatch(tiles, tiles[0].setup_kwargs()).allocate()
+    b.run(0, 1)
+    torch.cuda.synchronize()
+    ref = [b.image(p).clone() for p in range(int(b.info.n_pairs))]
+    cfg, ms, table = autotune.tune(b, reps=1)
+    assert cfg in table and ms > 0
+    b.run()
+    torch.cuda.synchronize()
+    for p in range(int(b.info.n_pairs)):
+        assert torch.equal(b.image(p), ref[p])
+    cfg2, _, table2 = autotune.tune(b)
+    assert cfg2 == cfg and table2 is None  # cached
+    b.close()

@@ -15,19 +15,25 @@ from fastpli_gb300.simulation import _Generator, _Simulator
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def header_functions():
-    src = open(os.path.join(ROOT, "include", "fastpli_gb300.h")).read()
+def header_functions(name):
+    src = open(os.path.join(ROOT, "include", name)).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
     return sorted(set(re.findall(r"\b(fpgb_[a-z0-9_]+)\s*\(", src)))
 
 
 def test_library_loads_and_exports_header_symbols():
+    from fastpli_gb300 import batch
     lib = fastpli_gb300.native_library()
-    names = header_functions()
-    assert len(names) >= 10
-    for n in names:
-        assert hasattr(lib, n), f"{n} declared in include/ but not exported"
-    assert set(names) == set(N.exported_symbols()), "ctypes table out of sync with header"
+    headers = sorted(f for f in os.listdir(os.path.join(ROOT, "include")) if f.endswith(".h"))
+    assert headers == ["fastpli_gb300.h", "fastpli_gb300_batch.h"]
+    tables = {"fastpli_gb300.h": N.exported_symbols(),
+              "fastpli_gb300_batch.h": batch.exported_symbols()}
+    for h in headers:
+        names = header_functions(h)
+        assert names
+        for n in names:
+            assert hasattr(lib, n), f"{n} declared in include/{h} but not exported"
+        assert set(names) == set(tables[h]), f"ctypes table out of sync with {h}"
     assert b"sm_103a" in lib.fpgb_version()
 
 
