@@ -29,7 +29,8 @@ LIB_PATH = os.path.join(OUT_DIR, LIB_NAME)
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
           "-I", os.path.join(ROOT, "include")]
-PER_FILE = {"tissue.cu": ["-fmad=false"], "batch_tissue.cu": ["-fmad=false"]}
+PER_FILE = {"tissue.cu": ["-fmad=false", "-Xcompiler", "-fopenmp"],
+            "batch_tissue.cu": ["-fmad=false"]}
 
 
 def _nvcc():
@@ -78,7 +79,7 @@ def build(force=False, verbose=False, extra=()):
             if err.strip():
                 print(err, file=sys.stderr)
     tmp = LIB_PATH + ".tmp"
-    cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
+    cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-lgomp"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -86,6 +86,7 @@ batch_march(const MarchParams *__restrict__ prm, const BatchItem *__restrict__ i
    // the item's parameter block, staged in shared memory (read like the
    // plain kernel reads its by-value parameters)
    __shared__ __align__(16) MarchParams sP;
+   __shared__ CoopScratch scratch[kBatchThreads / 32];
    int cur = -1;
    for (;;) {
       if (threadIdx.x == 0)
@@ -107,9 +108,20 @@ batch_march(const MarchParams *__restrict__ prm, const BatchItem *__restrict__ i
             cur = w.pair;
             __syncthreads();
          }
-         for (int r = threadIdx.x; r < w.ray_count; r += blockDim.x)
-            march_one_ray<MODE, TILT>(sP, w.ray_begin + r, sP.label, sP.vec, sP.image,
-                                      sP.epa_t, sP.epa_d, sP.epa_r, counters);
+         if (!TILT && sP.column) {
+            if ((int)threadIdx.x < w.ray_count)
+               march_one_ray_column(sP, w.ray_begin + threadIdx.x, sP.label, sP.vec, sP.image,
+                                    sP.epa_t, sP.epa_d, sP.epa_r, counters);
+         } else if (MODE == 0) {
+            if ((int)threadIdx.x < w.ray_count)
+               march_one_ray<MODE, TILT>(sP, w.ray_begin + threadIdx.x, sP.label, sP.vec,
+                                         sP.image, sP.epa_t, sP.epa_d, sP.epa_r, counters);
+         } else {
+            march_ray_coop<MODE, TILT>(sP, w.ray_begin + threadIdx.x,
+                                       (int)threadIdx.x < w.ray_count, sP.label, sP.vec,
+                                       sP.image, sP.epa_t, sP.epa_d, sP.epa_r, counters,
+                                       scratch[threadIdx.x >> 5]);
+         }
       }
       __syncthreads(); // s_item is rewritten for the next chunk
    }

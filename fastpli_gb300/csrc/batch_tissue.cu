@@ -92,9 +92,15 @@ batch_write(const unsigned long long *__restrict__ keys, const SegDev *__restric
    const unsigned *minb = min_bundle ? min_bundle + T.vox_base : nullptr;
    const unsigned long long *key = keys + T.vox_base;
    unsigned long long n_overflow = 0, n_overlap = 0, n_slow = 0;
-   const unsigned zz = (unsigned)T.Z, yy = (unsigned)T.Y;
-   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < T.n_vox;
-        i += (int64_t)gridDim.x * blockDim.x) {
+   // one warp per (x, y) row of the tile, lanes along z
+   const int lane = threadIdx.x & 31;
+   const int64_t n_rows = (int64_t)T.X * T.Y;
+   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+   for (int64_t row = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); row < n_rows;
+        row += warps) {
+   const int x = (int)(row / T.Y), y = (int)(row - (row / T.Y) * T.Y);
+   for (int z = lane; z < T.Z; z += 32) {
+      const int64_t i = row * T.Z + z;
       const unsigned long long k = key[i];
       if (k == ~0ull) {
          label[i] = 0;
@@ -107,8 +113,6 @@ batch_write(const unsigned long long *__restrict__ keys, const SegDev *__restric
       const float dist_squ = __uint_as_float((unsigned)(k >> 32));
       const SegDev &S = segs[seg];
       const LayerDev &L = layers[T.layer_base + S.bundle];
-      const unsigned ii = (unsigned)i, xy = ii / zz; // tiles hold < 2^32 voxels
-      const int z = (int)(ii - xy * zz), x = (int)(xy / yy), y = (int)(xy - (unsigned)x * yy);
       const float lpt[3] = {(float)(x - S.base[0]) + 0.5f, (float)(y - S.base[1]) + 0.5f,
                             (float)(z - S.base[2]) + 0.5f};
       FastCand fc;
@@ -165,6 +169,7 @@ batch_write(const unsigned long long *__restrict__ keys, const SegDev *__restric
       vec[3 * i + 1] = o[1];
       vec[3 * i + 2] = o[2];
    }
+   }
    if (n_overlap)
       atomicAdd(&counters[0], n_overlap);
    if (n_overflow)
@@ -184,8 +189,8 @@ int launch_batch_tissue(const SegDev *segs, const int32_t *seg_tile, int64_t n_s
       FPGB_CUDA_TRY(cudaGetLastError());
    }
    if (n_tiles > 0) {
-      const unsigned gx = (unsigned)std::max<int64_t>(
-          1, std::min<int64_t>((max_tile_voxels + 255) / 256, (int64_t)sms * 12 / n_tiles + 1));
+      (void)max_tile_voxels;
+      const unsigned gx = (unsigned)std::max<int64_t>(1, (int64_t)sms * 12 / n_tiles + 1);
       dim3 grid(gx, (unsigned)n_tiles);
       batch_write<<<grid, 256, 0, st>>>(keys, segs, tiles, layers, labels, vecs, min_bundle,
                                         counters);

@@ -58,6 +58,17 @@ FPGB_HD ff ff_add(ff a, ff b) {
 
 FPGB_HD ff ff_sub(ff a, ff b) { return ff_add(a, ff_neg(b)); }
 
+// Cheaper addition: the two low parts are added in one rounding.  Its error
+// is a few units of 2^-48 of |a| + |b| (not of the result), which is the
+// form every bound of the voxelizer's fast path is stated in.
+FPGB_HD ff ff_add_sloppy(ff a, ff b) {
+   ff s = two_sum(a.hi, b.hi);
+   s.lo += a.lo + b.lo;
+   return quick_two_sum(s.hi, s.lo);
+}
+
+FPGB_HD ff ff_sub_sloppy(ff a, ff b) { return ff_add_sloppy(a, ff_neg(b)); }
+
 FPGB_HD ff ff_add_f(ff a, float b) {
    ff s = two_sum(a.hi, b);
    s.lo += a.lo;
@@ -98,6 +109,23 @@ FPGB_HD ff ff_sqrt(ff a) {
    const float s = sqrtf(a.hi);
    const ff r = ff_sub(a, two_prod(s, s));
    return quick_two_sum(s, r.hi / (2.f * s));
+}
+
+// a / b given r ~ 1/b (any float within a few ulp): two residual
+// corrections of the FP32 quotient, no division instruction.
+FPGB_HD ff ff_div_rcp(ff a, ff b, float r) {
+   const float q1 = a.hi * r;
+   const ff e1 = ff_sub_sloppy(a, ff_mul_f(b, q1));
+   const float q2 = e1.hi * r;
+   const ff e2 = ff_sub_sloppy(e1, ff_mul_f(b, q2));
+   const float q3 = e2.hi * r;
+   return ff_add_f(quick_two_sum(q1, q2), q3);
+}
+
+FPGB_HD ff ff_norm2_sloppy(const ff a[3]) {
+   ff s = ff_sqr(a[0]);
+   s = ff_add_sloppy(s, ff_sqr(a[1]));
+   return ff_add_sloppy(s, ff_sqr(a[2]));
 }
 
 FPGB_HD ff ff_dot3(const ff a[3], const ff b[3]) {

@@ -130,10 +130,10 @@ __device__ F3 axis_interp(const MarchParams &P, const int32_t *__restrict__ labe
          continue;
       const int64_t xi = (k & 1) ? x1 : x0, yi = (k & 2) ? y1 : y0, zi = (k & 4) ? z1 : z0;
       const int64_t idx = xi * YZ + yi * P.Z + zi;
-      if (__ldg(label + idx) == lab)
-         c[k] = load_vec(vec, idx);
-      else
-         c[k] = F3{0.f, 0.f, 0.f};
+      // GetVec(...) * (GetLabel(...) == label) (simulator.cpp:533-540)
+      const float m = (__ldg(label + idx) == lab) ? 1.f : 0.f;
+      const F3 u = load_vec(vec, idx);
+      c[k] = F3{u.x * m, u.y * m, u.z * m};
    }
    F3 c00 = c[0], c10 = c[2], c01 = c[4], c11 = c[6];
    if (ax) {
@@ -281,9 +281,94 @@ __device__ __forceinline__ void retard(float &u1, float &u2, float &u3, F3 v, fl
    }
 }
 
-// One CCD-pixel ray: start, march, analyser and the rho/epa epilogue.  Used
-// by the plain per-call kernel and by the persistent batched kernel, so both
-// produce bit-identical images.
+// Analyser and the rho / epa epilogue of one ray (simulator.cpp:346-362,
+// epa.py:31-43), plus its warning / status counters.
+__device__ __forceinline__ void ray_epilogue(const MarchParams &P, int64_t ray, float u1, float u2,
+                                             float L, double *__restrict__ image,
+                                             double *__restrict__ epa_t,
+                                             double *__restrict__ epa_d,
+                                             double *__restrict__ epa_r, bool w_zero,
+                                             bool w_norm, bool bad_label,
+                                             unsigned long long *__restrict__ counters) {
+   const float amp = P.i4 * expf(-L);
+   float a0 = 0.f, a1 = 0.f, b1 = 0.f;
+   double *out = image + ray * P.n_rho;
+   for (int r = 0; r < P.n_rho; r++) {
+      const float I = amp * (1.f - u1 * P.c2r[r] + u2 * P.s2r[r]);
+      if (image)
+         out[r] = widen(I);
+      a0 += I;
+      a1 += I * P.epa_sin[r];
+      b1 += I * P.epa_cos[r];
+   }
+   if (epa_t || epa_d || epa_r) {
+      const float n = (float)P.n_rho;
+      a0 = a0 / n;
+      a1 = 2.f * a1 / n;
+      b1 = 2.f * b1 / n;
+      if (epa_t)
+         epa_t[ray] = widen(2.f * a0);
+      if (epa_d) {
+         float d = 0.5f * atan2f(-b1, a1) + 3.14159265358979f;
+         if (d >= 3.14159265358979f)
+            d -= 3.14159265358979f;
+         epa_d[ray] = widen(d);
+      }
+      if (epa_r) {
+         if (a0 < 2.220446e-14f)
+            a0 = 1.f;
+         epa_r[ray] = widen(sqrtf(a1 * a1 + b1 * b1) / a0);
+      }
+   }
+   if (w_zero)
+      atomicAdd(&counters[2], 1ull);
+   if (w_norm)
+      atomicAdd(&counters[3], 1ull);
+   if (bad_label)
+      atomicOr(&counters[6], (unsigned long long)kStatusLabelRange);
+}
+
+// Fixed-point start of ray `ray` (CCD pixel x = ray / Y, y = ray % Y).
+__device__ __forceinline__ void ray_setup(const MarchParams &P, int64_t ray, int64_t &px,
+                                          int64_t &py) {
+   const int64_t cx = ray / P.Y, cy = ray - (ray / P.Y) * P.Y;
+   double sx, sy;
+   ray_start(P, cx, cy, sx, sy);
+   px = to_fixed(sx, P.frac_bits);
+   py = to_fixed(sy, P.frac_bits);
+}
+
+// The rotation of one birefringent step, from the (tilted) optic axis v and
+// |v_untilted|^2 = n2: cos 2phi, sin 2phi, cos ret, sin ret
+// (simulator.cpp:309-320).  Returns false when vx = vy = 0 (no rotation).
+__device__ __forceinline__ bool retard_params(F3 v, float n2, float kret, float &c, float &s,
+                                              float &cr, float &sr) {
+   const float xx = v.x * v.x, yy = v.y * v.y;
+   const float q = xx + yy;
+   if (!(q > 0.f))
+      return false;
+   const float ret = kret * q * rsqrtf(n2);
+   sincos_small(ret, sr, cr);
+   const float iq = __fdividef(1.f, q);
+   c = (xx - yy) * iq;
+   s = 2.f * v.x * v.y * iq;
+   return true;
+}
+
+// Apply R(-2phi) Ret R(2phi) to the unit state (simulator.cpp:322-336 in the
+// rho-free frame).
+__device__ __forceinline__ void apply_retard(float &u1, float &u2, float &u3, float c, float s,
+                                             float cr, float sr) {
+   const float a1 = u1 * c - u2 * s;
+   const float c1 = u1 * s + u2 * c;
+   const float b1 = c1 * cr + u3 * sr;
+   u3 = -c1 * sr + u3 * cr;
+   u1 = a1 * c + b1 * s;
+   u2 = -a1 * s + b1 * c;
+}
+
+// One CCD-pixel ray, one thread, every step in order.  Used for NN, where a
+// birefringent step costs one vector load.
 template <int MODE, bool TILT>
 __device__ __forceinline__ void march_one_ray(const MarchParams &P, int64_t ray,
                                               const int32_t *__restrict__ label,
@@ -293,15 +378,9 @@ __device__ __forceinline__ void march_one_ray(const MarchParams &P, int64_t ray,
                                               double *__restrict__ epa_d,
                                               double *__restrict__ epa_r,
                                               unsigned long long *__restrict__ counters) {
-   const int64_t cx = ray / P.Y, cy = ray - (ray / P.Y) * P.Y;
    const int F = P.frac_bits;
    int64_t px, py;
-   {
-      double sx, sy;
-      ray_start(P, cx, cy, sx, sy);
-      px = to_fixed(sx, F);
-      py = to_fixed(sy, F);
-   }
+   ray_setup(P, ray, px, py);
    const int64_t YZ = P.Y * P.Z;
    float u1 = 0.f, u2 = 0.f, u3 = -1.f, L = 0.f;
    bool w_zero = false, w_norm = false, bad_label = false;
@@ -350,46 +429,313 @@ __device__ __forceinline__ void march_one_ray(const MarchParams &P, int64_t ray,
                 P.rot[3] * v.x + P.rot[4] * v.y + P.rot[5] * v.z,
                 P.rot[6] * v.x + P.rot[7] * v.y + P.rot[8] * v.z};
       }
-      retard(u1, u2, u3, v, n2, o.kret);
+      float c, s, cr, sr;
+      if (retard_params(v, n2, o.kret, c, s, cr, sr))
+         apply_retard(u1, u2, u3, c, s, cr, sr);
       L += o.alog;
    }
-   // analyser and the rho epilogue (simulator.cpp:346-362)
-   const float amp = P.i4 * expf(-L);
-   float a0 = 0.f, a1 = 0.f, b1 = 0.f;
-   double *out = image + ray * P.n_rho;
-   for (int r = 0; r < P.n_rho; r++) {
-      const float I = amp * (1.f - u1 * P.c2r[r] + u2 * P.s2r[r]);
-      if (image)
-         out[r] = widen(I);
-      a0 += I;
-      a1 += I * P.epa_sin[r];
-      b1 += I * P.epa_cos[r];
-   }
-   if (epa_t || epa_d || epa_r) { // epa.py:31-43
-      const float n = (float)P.n_rho;
-      a0 = a0 / n;
-      a1 = 2.f * a1 / n;
-      b1 = 2.f * b1 / n;
-      if (epa_t)
-         epa_t[ray] = widen(2.f * a0);
-      if (epa_d) {
-         float d = 0.5f * atan2f(-b1, a1) + 3.14159265358979f;
-         if (d >= 3.14159265358979f)
-            d -= 3.14159265358979f;
-         epa_d[ray] = widen(d);
+   ray_epilogue(P, ray, u1, u2, L, image, epa_t, epa_d, epa_r, w_zero, w_norm, bad_label,
+                counters);
+}
+
+// Vertical ray through its whole column in order (MarchParams::column):
+// labels and axes stream in as 16-byte loads, four voxels at a time (the
+// column starts 16-byte aligned because Z % 4 == 0).  Same arithmetic per
+// step as march_one_ray.  Interpolation modes need nothing else here: at the
+// exact voxel centres of such a ray every interpolation axis collapses.
+__device__ __forceinline__ void march_one_ray_column(const MarchParams &P, int64_t ray,
+                                                     const int32_t *__restrict__ label,
+                                                     const float *__restrict__ vec,
+                                                     double *__restrict__ image,
+                                                     double *__restrict__ epa_t,
+                                                     double *__restrict__ epa_d,
+                                                     double *__restrict__ epa_r,
+                                                     unsigned long long *__restrict__ counters) {
+   const int64_t base = ray * P.Z; // ray = cx * Y + cy: its column (cx, cy, 0..Z-1)
+   const int4 *lab4 = reinterpret_cast<const int4 *>(label + base);
+   const float4 *vec4 = reinterpret_cast<const float4 *>(vec + 3 * base);
+   float u1 = 0.f, u2 = 0.f, u3 = -1.f, L = 0.f;
+   bool w_zero = false, w_norm = false, bad_label = false;
+   const int nq = (int)(P.Z >> 2);
+   // the next quad's loads are issued before the current quad is processed
+   int q = P.flip_z ? nq - 1 : 0; // mirrored columns are read backwards
+   int4 nl = __ldg(lab4 + q);
+   float4 na = __ldg(vec4 + 3 * q), nb = __ldg(vec4 + 3 * q + 1), nc = __ldg(vec4 + 3 * q + 2);
+   for (int qi = 0; qi < nq; qi++) {
+      const int4 l4 = nl;
+      const float4 a = na, b = nb, c = nc;
+      if (qi + 1 < nq) {
+         q = P.flip_z ? nq - 2 - qi : qi + 1;
+         nl = __ldg(lab4 + q);
+         na = __ldg(vec4 + 3 * q);
+         nb = __ldg(vec4 + 3 * q + 1);
+         nc = __ldg(vec4 + 3 * q + 2);
       }
-      if (epa_r) {
-         if (a0 < 2.220446e-14f)
-            a0 = 1.f;
-         epa_r[ray] = widen(sqrtf(a1 * a1 + b1 * b1) / a0);
+      const int labs[4] = {l4.x, l4.y, l4.z, l4.w};
+      const F3 vs[4] = {F3{a.x, a.y, a.z}, F3{a.w, b.x, b.y}, F3{b.z, b.w, c.x},
+                        F3{c.y, c.z, c.w}};
+#pragma unroll
+      for (int jj = 0; jj < 4; jj++) {
+         const int j = P.flip_z ? 3 - jj : jj;
+         int lab = labs[j];
+         if (lab < 0 || lab >= P.n_props) {
+            bad_label = true;
+            lab = 0;
+         }
+         const LabelOptics o = P.lut[lab];
+         if (o.kind == 0)
+            continue;
+         if (o.kind == 1) {
+            L += o.alog;
+            continue;
+         }
+         const F3 v = vs[j];
+         if (is_zero(v)) {
+            w_zero = true;
+            continue;
+         }
+         const float n2 = dot3(v, v);
+         if (n2 - 1.f > 1e-5f)
+            w_norm = true;
+         float cc, ss, cr, sr;
+         if (retard_params(v, n2, o.kret, cc, ss, cr, sr))
+            apply_retard(u1, u2, u3, cc, ss, cr, sr);
+         L += o.alog;
       }
    }
-   if (w_zero)
-      atomicAdd(&counters[2], 1ull);
-   if (w_norm)
-      atomicAdd(&counters[3], 1ull);
-   if (bad_label)
-      atomicOr(&counters[6], (unsigned long long)kStatusLabelRange);
+   ray_epilogue(P, ray, u1, u2, L, image, epa_t, epa_d, epa_r, w_zero, w_norm, bad_label,
+                counters);
+}
+
+// ----------------------------------------------------------------------------
+// Warp-cooperative march for Lerp/Slerp.  Interpolating the optic axis of a
+// birefringent step costs ~20x a plain step, and within a warp different rays
+// need it at different steps, so a one-ray-per-thread loop pays it on almost
+// every step.  Here each warp takes its 32 rays through kCoopSteps steps at a
+// time in three phases:
+//   1. every lane classifies its steps (label, optics) and writes one job
+//      descriptor per birefringent step into shared memory;
+//   2. the warp's jobs are compacted and shared out to all 32 lanes, each job
+//      producing that step's rotation (cos 2phi, sin 2phi, cos/sin ret) from
+//      the interpolated axis — the interpolated axis of a step depends only on
+//      its position, not on the state;
+//   3. every lane applies its steps' rotations and attenuations in order.
+// The arithmetic per step is the same as march_one_ray's.
+// ----------------------------------------------------------------------------
+constexpr int kCoopSteps = 8;
+constexpr int kCoopSlots = kCoopSteps * 32; // per warp
+constexpr int kCoopFields = 8;
+
+struct CoopScratch {
+   float f[kCoopFields][kCoopSlots]; // slot = step * 32 + lane
+   unsigned short list[kCoopSlots];
+};
+
+// job status codes written to field 4
+constexpr int kJobRotate = 0, kJobIdentity = 1, kJobZero = 2, kJobNorm = 4;
+
+// One out-of-line copy of the pairwise interpolation for the cooperative job
+// (up to seven calls per job; inlining them all overflows the instruction
+// cache).
+template <int MODE>
+__device__ __noinline__ F3 interp_axis_call(F3 v, F3 u, float t) {
+   return interp_axis<MODE>(v, u, t);
+}
+
+template <int MODE, bool TILT>
+__device__ __forceinline__ void coop_job(const MarchParams &P, const int32_t *__restrict__ label,
+                                         const float *__restrict__ vec, CoopScratch &S,
+                                         int slot) {
+   const int x0 = __float_as_int(S.f[0][slot]);
+   const int y0 = __float_as_int(S.f[1][slot]);
+   const int z0 = __float_as_int(S.f[2][slot]);
+   const int fl = __float_as_int(S.f[3][slot]);
+   const float xd = S.f[4][slot], yd = S.f[5][slot], zd = S.f[6][slot];
+   const int lab = __float_as_int(S.f[7][slot]);
+   const bool ax = fl & 1, ay = fl & 2, az = fl & 4;
+   const int z1 = z0 + ((fl >> 3) & 3) - 1;
+   const int64_t YZ = P.Y * P.Z;
+   F3 v;
+   if (!ax && !ay && !az) {
+      v = load_vec(vec, (int64_t)x0 * YZ + (int64_t)y0 * P.Z + z0);
+   } else {
+      F3 c[8];
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+         if (((k & 1) && !ax) || ((k & 2) && !ay) || ((k & 4) && !az))
+            continue;
+         const int xi = x0 + (k & 1), yi = y0 + ((k >> 1) & 1), zi = (k & 4) ? z1 : z0;
+         const int64_t idx = (int64_t)xi * YZ + (int64_t)yi * P.Z + zi;
+         // GetVec(...) * (GetLabel(...) == label) (simulator.cpp:533-540);
+         // label and axis loads are issued together
+         const float m = (__ldg(label + idx) == lab) ? 1.f : 0.f;
+         const F3 u = load_vec(vec, idx);
+         c[k] = F3{u.x * m, u.y * m, u.z * m};
+      }
+      F3 c00 = c[0], c10 = c[2], c01 = c[4], c11 = c[6];
+      if (ax) {
+         c00 = interp_axis_call<MODE>(c[0], c[1], xd);
+         if (az)
+            c01 = interp_axis_call<MODE>(c[4], c[5], xd);
+         if (ay) {
+            c10 = interp_axis_call<MODE>(c[2], c[3], xd);
+            if (az)
+               c11 = interp_axis_call<MODE>(c[6], c[7], xd);
+         }
+      }
+      F3 c0 = c00, c1 = c01;
+      if (ay) {
+         c0 = interp_axis_call<MODE>(c00, c10, yd);
+         if (az)
+            c1 = interp_axis_call<MODE>(c01, c11, yd);
+      }
+      v = az ? interp_axis_call<MODE>(c0, c1, zd) : c0;
+   }
+   int status;
+   float c = 1.f, s = 0.f, cr = 1.f, sr = 0.f;
+   if (is_zero(v)) {
+      status = kJobZero;
+   } else {
+      const float n2 = dot3(v, v);
+      status = (n2 - 1.f > 1e-5f) ? kJobNorm : 0;
+      if (TILT && P.rotate) {
+         v = F3{P.rot[0] * v.x + P.rot[1] * v.y + P.rot[2] * v.z,
+                P.rot[3] * v.x + P.rot[4] * v.y + P.rot[5] * v.z,
+                P.rot[6] * v.x + P.rot[7] * v.y + P.rot[8] * v.z};
+      }
+      if (!retard_params(v, n2, P.lut[lab].kret, c, s, cr, sr))
+         status |= kJobIdentity;
+   }
+   S.f[0][slot] = c;
+   S.f[1][slot] = s;
+   S.f[2][slot] = cr;
+   S.f[3][slot] = sr;
+   S.f[4][slot] = __int_as_float(status);
+}
+
+template <int MODE, bool TILT>
+__device__ __forceinline__ void march_ray_coop(const MarchParams &P, int64_t ray, bool active,
+                                               const int32_t *__restrict__ label,
+                                               const float *__restrict__ vec,
+                                               double *__restrict__ image,
+                                               double *__restrict__ epa_t,
+                                               double *__restrict__ epa_d,
+                                               double *__restrict__ epa_r,
+                                               unsigned long long *__restrict__ counters,
+                                               CoopScratch &S) {
+   const int lane = threadIdx.x & 31;
+   const int F = P.frac_bits;
+   const int64_t YZ = P.Y * P.Z;
+   int64_t px = 0, py = 0;
+   if (active)
+      ray_setup(P, ray, px, py);
+   const int64_t half = int64_t(1) << (F - 1);
+   const uint64_t mask = (uint64_t(1) << F) - 1;
+   const float scale = __int_as_float((127 - F) << 23); // 2^-F
+   float u1 = 0.f, u2 = 0.f, u3 = -1.f, L = 0.f;
+   bool w_zero = false, w_norm = false, bad_label = false;
+   for (int k0 = 0; k0 < P.n_z; k0 += kCoopSteps) {
+      // phase 1: classify this lane's steps, write job descriptors
+      unsigned kinds = 0; // 2 bits per step
+      float alog[kCoopSteps];
+#pragma unroll
+      for (int j = 0; j < kCoopSteps; j++) {
+         const int k = k0 + j;
+         alog[j] = 0.f;
+         if (!active || k >= P.n_z)
+            continue;
+         if (TILT && k > 0) {
+            px += P.dx_fx;
+            py += P.dy_fx;
+         }
+         const int64_t ix = px >> F, iy = py >> F;
+         const ZStep zs = P.ztab[k];
+         int lab = 0;
+         if (ix >= 0 && ix < P.X && iy >= 0 && iy < P.Y) {
+            lab = __ldg(label + ix * YZ + iy * P.Z + zs.iz);
+            if (lab < 0 || lab >= P.n_props) {
+               bad_label = true;
+               lab = 0;
+            }
+         }
+         const LabelOptics o = P.lut[lab];
+         alog[j] = o.alog;
+         kinds |= (unsigned)o.kind << (2 * j);
+         if (o.kind != 2)
+            continue;
+         // trilinear corners as in axis_interp (simulator.cpp:510-530)
+         const int64_t hx = px - half, hy = py - half;
+         const int64_t fx0 = hx >> F, fy0 = hy >> F;
+         const float xf = (float)(int64_t)((uint64_t)hx & mask) * scale;
+         const float yf = (float)(int64_t)((uint64_t)hy & mask) * scale;
+         const int64_t x0 = clampi(fx0, P.X - 1), x1 = clampi(fx0 + (xf != 0.f), P.X - 1);
+         const int64_t y0 = clampi(fy0, P.Y - 1), y1 = clampi(fy0 + (yf != 0.f), P.Y - 1);
+         int64_t z0 = clampi(zs.z0, P.Z - 1), z1 = clampi((int64_t)zs.z0 + (zs.zf != 0.f), P.Z - 1);
+         const float zd = (z0 != z1) ? zs.zf : 0.f;
+         if (P.flip_z) {
+            z0 = P.Z - 1 - z0;
+            z1 = P.Z - 1 - z1;
+         }
+         const int ax = x0 != x1, ay = y0 != y1, az = z0 != z1;
+         const int slot = j * 32 + lane;
+         S.f[0][slot] = __int_as_float((int)x0);
+         S.f[1][slot] = __int_as_float((int)y0);
+         S.f[2][slot] = __int_as_float((int)z0);
+         S.f[3][slot] = __int_as_float(ax | (ay << 1) | (az << 2) | ((int)(z1 - z0 + 1) << 3));
+         S.f[4][slot] = ax ? xf : 0.f;
+         S.f[5][slot] = ay ? yf : 0.f;
+         S.f[6][slot] = zd;
+         S.f[7][slot] = __int_as_float(lab);
+      }
+      // phase 2: compact the warp's jobs and share them out
+      unsigned jobs = 0;
+#pragma unroll
+      for (int j = 0; j < kCoopSteps; j++)
+         jobs |= (((kinds >> (2 * j)) & 3u) == 2u) ? (1u << j) : 0u;
+      const int cnt = __popc(jobs);
+      int pre = cnt;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+         const int v = __shfl_up_sync(0xffffffffu, pre, o);
+         if (lane >= o)
+            pre += v;
+      }
+      const int total = __shfl_sync(0xffffffffu, pre, 31);
+      pre -= cnt;
+      for (unsigned m = jobs; m; m &= m - 1) {
+         const int j = __ffs(m) - 1;
+         S.list[pre++] = (unsigned short)(j * 32 + lane);
+      }
+      __syncwarp();
+      for (int t = lane; t < total; t += 32)
+         coop_job<MODE, TILT>(P, label, vec, S, S.list[t]);
+      __syncwarp();
+      // phase 3: apply this lane's steps in order
+#pragma unroll
+      for (int j = 0; j < kCoopSteps; j++) {
+         const unsigned kind = (kinds >> (2 * j)) & 3u;
+         if (kind == 1u) {
+            L += alog[j];
+         } else if (kind == 2u) {
+            const int slot = j * 32 + lane;
+            const int st = __float_as_int(S.f[4][slot]);
+            if (st & kJobZero) { // simulator.cpp:292-297: no attenuation either
+               w_zero = true;
+               continue;
+            }
+            if (st & kJobNorm)
+               w_norm = true;
+            if (!(st & kJobIdentity))
+               apply_retard(u1, u2, u3, S.f[0][slot], S.f[1][slot], S.f[2][slot],
+                            S.f[3][slot]);
+            L += alog[j];
+         }
+      }
+      __syncwarp(); // the scratch is rewritten by the next block of steps
+   }
+   if (active)
+      ray_epilogue(P, ray, u1, u2, L, image, epa_t, epa_d, epa_r, w_zero, w_norm, bad_label,
+                   counters);
 }
 
 } // namespace fpgb

@@ -260,6 +260,19 @@ int plan_march(const fpgb_setup *s, const int64_t *dim, const double *props, int
       plan->ztab.push_back(zs);
    }
    P.n_z = (int32_t)plan->ztab.size();
+   // vertical rays that visit every z of their column in order: theta = 0
+   // with step 1 (simulator.cpp:259-261 then gives z = k + 1/2); at those
+   // exact voxel centres Lerp and Slerp reduce to the voxel's own axis
+   // (simulator.cpp:518-519)
+   P.column = 0;
+   if (theta == 0 && P.n_z == P.Z && P.Z % 4 == 0 && step[0] == 0 && step[1] == 0) {
+      bool seq = true;
+      for (int32_t k = 0; k < P.n_z && seq; k++) {
+         const ZStep &zs = plan->ztab[k];
+         seq = zs.iz == (P.flip_z ? P.Z - 1 - k : k) && zs.zf == 0.f && zs.z0 == k;
+      }
+      P.column = seq ? 1 : 0;
+   }
    plan->steps = P.X * P.Y * (int64_t)P.n_z;
 
    // fixed-point format for x/y: enough integer bits for every position a
@@ -301,9 +314,18 @@ march_rays(const MarchParams P, const int32_t *__restrict__ label,
            double *__restrict__ epa_t, double *__restrict__ epa_d, double *__restrict__ epa_r,
            unsigned long long *__restrict__ counters) {
    const int64_t ray = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-   if (ray >= P.X * P.Y)
-      return;
-   march_one_ray<MODE, TILT>(P, ray, label, vec, image, epa_t, epa_d, epa_r, counters);
+   if (!TILT && P.column) {
+      if (ray < P.X * P.Y)
+         march_one_ray_column(P, ray, label, vec, image, epa_t, epa_d, epa_r, counters);
+   } else if (MODE == 0) {
+      if (ray >= P.X * P.Y)
+         return;
+      march_one_ray<MODE, TILT>(P, ray, label, vec, image, epa_t, epa_d, epa_r, counters);
+   } else { // whole warps take part in the cooperative march
+      __shared__ CoopScratch scratch[4];
+      march_ray_coop<MODE, TILT>(P, ray, ray < P.X * P.Y, label, vec, image, epa_t, epa_d,
+                                 epa_r, counters, scratch[threadIdx.x >> 5]);
+   }
 }
 
 // Full-volume label range check (simulator.cpp:149-167).
@@ -362,6 +384,8 @@ int launch_march(const MarchPlan &mp, const int32_t *d_label, const float *d_vec
                                  cudaMemcpyHostToDevice, st));
    P.lut = lut;
    P.ztab = zt;
+   if (reinterpret_cast<uintptr_t>(d_label) % 16 || reinterpret_cast<uintptr_t>(d_vec) % 16)
+      P.column = 0;
    const int64_t n_rays = P.X * P.Y;
    const unsigned grid = (unsigned)((n_rays + 127) / 128);
    const bool tilt = P.rotate || P.dx_fx != 0 || P.dy_fx != 0;

@@ -52,7 +52,8 @@ struct MarchParams {
    const float *vec;
    double *image, *epa_t, *epa_d, *epa_r;
    int32_t tilted; // x/y advance or the axis rotates
-   int32_t pad_;
+   int32_t column; // vertical ray reading z = 0..Z-1 (or mirrored) in order,
+                   // Z % 4 == 0: the vectorised column path applies
 };
 
 struct MarchPlan {

@@ -118,6 +118,7 @@ void fill_fast_fields(SegDev &S, const fpgb_volume *vol) {
    }
    S.pscale = (float)(ps + 2.0);
    split2(S.c2, S.c2_hi, S.c2_lo);
+   S.c2_rcp = S.c2 > 0 ? (float)(1.0 / S.c2) : 0.f;
    split2(S.r0, S.r0_hi, S.r0_lo);
    split2(S.r1 - S.r0, S.dr_hi, S.dr_lo);
    // Fiber::CalcRadius at t = 0 and t = 1 is exactly r0 and r1
@@ -280,86 +281,124 @@ int plan_tissue(const fpgb_volume *vol, const fpgb_fibers *fb, TissuePlan *plan)
       volbox.mx[i] = (double)vol->dim[i];
    }
 
-   // segment table in the reference's processing order (generator.cpp:205-231)
-   int64_t cand = 0;
+   // segment table in the reference's processing order (generator.cpp:205-231):
+   // which bundles overlap the volume is decided first, then the fibers are
+   // planned in parallel into per-fiber lists that are concatenated in order
+   std::vector<char> bundle_on(nb > 0 ? nb : 1, 0);
+   std::vector<int32_t> fiber_bundle(nf);
    for (int64_t b = 0; b < nb; b++) {
       const int64_t f0 = fb->bundle_fiber_off[b], f1 = fb->bundle_fiber_off[b + 1];
       Box bb;
       bb.empty(); // fiber_bundle.cpp:147-154
       if (f1 > f0)
          bb = fbox[f0];
-      for (int64_t fi = f0; fi < f1; fi++)
-         bb.unite(fbox[fi]);
-      if (!overlap(volbox, bb))
-         continue;
-      const LayerDev &L = plan->layers[b];
       for (int64_t fi = f0; fi < f1; fi++) {
-         const int64_t p0 = fb->fiber_point_off[fi], p1 = fb->fiber_point_off[fi + 1];
-         if (p1 - p0 <= 1) {
-            plan->single_point++;
+         bb.unite(fbox[fi]);
+         fiber_bundle[fi] = (int32_t)b;
+      }
+      bundle_on[b] = overlap(volbox, bb) ? 1 : 0;
+   }
+   // pass 1: segments each fiber keeps (its boxes only); pass 2 fills the
+   // table in place at the fibers' prefix offsets
+   std::vector<int64_t> fiber_segs(nf + 1, 0);
+   std::vector<char> single(nf, 0);
+   auto seg_box = [&](int64_t s, double rsl, SegDev &S) -> int64_t {
+      const double *P = &xyz[3 * s], *Q = &xyz[3 * (s + 1)];
+      const double r0 = rad[s], r1 = rad[s + 1];
+      const double rmax = (r0 < r1 ? r1 : r0) * rsl;
+      Box sb;
+      sb.from_pq(P, Q);
+      int64_t count = 1;
+      for (int i = 0; i < 3; i++) {
+         sb.mn[i] -= rmax;
+         sb.mx[i] += rmax;
+         if (volbox.mn[i] > sb.mn[i])
+            sb.mn[i] = volbox.mn[i];
+         if (volbox.mx[i] < sb.mx[i])
+            sb.mx[i] = volbox.mx[i];
+         if (!(sb.mn[i] <= sb.mx[i])) { // empty or non-finite box
+            S.lo[i] = 0;
+            S.ext[i] = 0;
+            count = 0;
             continue;
          }
-         if (!overlap(volbox, fbox[fi]))
+         // (int64) truncation as generator.cpp:304-305; the clamp only
+         // restates that the box already lies in [0, dim]
+         const int64_t lo = std::max<int64_t>(0, (int64_t)sb.mn[i]);
+         const int64_t hi = std::min<int64_t>(vol->dim[i], (int64_t)(sb.mx[i] + 0.5));
+         S.lo[i] = (int32_t)lo;
+         S.ext[i] = (int32_t)(hi > lo ? hi - lo : 0);
+         count *= S.ext[i];
+      }
+      return count;
+   };
+   auto fiber_used = [&](int64_t fi) -> bool {
+      const int64_t b = fiber_bundle[fi];
+      const int64_t p0 = fb->fiber_point_off[fi], p1 = fb->fiber_point_off[fi + 1];
+      return bundle_on[b] && p1 - p0 > 1 && overlap(volbox, fbox[fi]) && plan->layers[b].n > 0;
+   };
+#pragma omp parallel for schedule(dynamic, 32)
+   for (int64_t fi = 0; fi < nf; fi++) {
+      const int64_t b = fiber_bundle[fi];
+      const int64_t p0 = fb->fiber_point_off[fi], p1 = fb->fiber_point_off[fi + 1];
+      if (bundle_on[b] && p1 - p0 <= 1)
+         single[fi] = 1;
+      if (!fiber_used(fi))
+         continue;
+      int64_t n = 0;
+      SegDev S;
+      for (int64_t s = p0; s + 1 < p1; s++)
+         n += seg_box(s, plan->layers[b].sqrt_last, S) > 0;
+      fiber_segs[fi + 1] = n;
+   }
+   for (int64_t fi = 0; fi < nf; fi++) {
+      fiber_segs[fi + 1] += fiber_segs[fi];
+      plan->single_point += single[fi];
+   }
+   plan->segs.reset((size_t)fiber_segs[nf]);
+   SegDev *table = plan->segs.data();
+   int64_t cand = 0;
+#pragma omp parallel for schedule(dynamic, 32) reduction(+ : cand)
+   for (int64_t fi = 0; fi < nf; fi++) {
+      if (!fiber_used(fi))
+         continue;
+      const int64_t b = fiber_bundle[fi];
+      const LayerDev &L = plan->layers[b];
+      const int64_t p0 = fb->fiber_point_off[fi], p1 = fb->fiber_point_off[fi + 1];
+      int64_t at = fiber_segs[fi];
+      for (int64_t s = p0; s + 1 < p1; s++) {
+         SegDev S;
+         std::memset(&S, 0, sizeof S);
+         const int64_t count = seg_box(s, L.sqrt_last, S);
+         if (count == 0)
             continue;
-         if (L.n == 0)
-            continue;
-         for (int64_t s = p0; s + 1 < p1; s++) {
-            const double *P = &xyz[3 * s], *Q = &xyz[3 * (s + 1)];
-            const double r0 = rad[s], r1 = rad[s + 1];
-            const double rmax = (r0 < r1 ? r1 : r0) * L.sqrt_last;
-            Box sb;
-            sb.from_pq(P, Q);
-            SegDev S{};
-            int64_t count = 1;
-            for (int i = 0; i < 3; i++) {
-               sb.mn[i] -= rmax;
-               sb.mx[i] += rmax;
-               if (volbox.mn[i] > sb.mn[i])
-                  sb.mn[i] = volbox.mn[i];
-               if (volbox.mx[i] < sb.mx[i])
-                  sb.mx[i] = volbox.mx[i];
-               if (!(sb.mn[i] <= sb.mx[i])) { // empty or non-finite box
-                  count = 0;
-                  S.lo[i] = 0;
-                  S.ext[i] = 0;
-                  continue;
-               }
-               // (int64) truncation as generator.cpp:304-305; the clamp only
-               // restates that the box already lies in [0, dim]
-               const int64_t lo = std::max<int64_t>(0, (int64_t)sb.mn[i]);
-               const int64_t hi = std::min<int64_t>(vol->dim[i], (int64_t)(sb.mx[i] + 0.5));
-               S.lo[i] = (int32_t)lo;
-               S.ext[i] = (int32_t)(hi > lo ? hi - lo : 0);
-               count *= S.ext[i];
-            }
-            if (count == 0)
-               continue;
-            for (int i = 0; i < 3; i++) {
-               S.p[i] = P[i];
-               S.q[i] = Q[i];
-               S.v[i] = Q[i] - P[i];
-               const double base = std::floor(P[i]);
-               S.base[i] = (int32_t)std::max(-2147483647.0, std::min(2147483647.0, base));
-               S.pf[i] = (float)(P[i] - (double)S.base[i]);
-               S.vf[i] = (float)S.v[i];
-            }
-            {
-               double c = 0.0;
-               c = c + S.v[0] * S.v[0];
-               c = c + S.v[1] * S.v[1];
-               c = c + S.v[2] * S.v[2];
-               S.c2 = c;
-            }
-            S.c2f = (float)S.c2;
-            S.r0 = r0;
-            S.r1 = r1;
-            fill_fast_fields(S, vol);
-            const double rm = r0 < r1 ? r1 : r0;
-            S.thr_f = (float)((double)L.f_ly_squ * rm * rm * (1.0 + 1e-3) + 1e-3);
-            S.bundle = (int32_t)b;
-            plan->segs.push_back(S);
-            cand += count;
+         const double *P = &xyz[3 * s], *Q = &xyz[3 * (s + 1)];
+         const double r0 = rad[s], r1 = rad[s + 1];
+         for (int i = 0; i < 3; i++) {
+            S.p[i] = P[i];
+            S.q[i] = Q[i];
+            S.v[i] = Q[i] - P[i];
+            const double base = std::floor(P[i]);
+            S.base[i] = (int32_t)std::max(-2147483647.0, std::min(2147483647.0, base));
+            S.pf[i] = (float)(P[i] - (double)S.base[i]);
+            S.vf[i] = (float)S.v[i];
          }
+         {
+            double c = 0.0;
+            c = c + S.v[0] * S.v[0];
+            c = c + S.v[1] * S.v[1];
+            c = c + S.v[2] * S.v[2];
+            S.c2 = c;
+         }
+         S.c2f = (float)S.c2;
+         S.r0 = r0;
+         S.r1 = r1;
+         fill_fast_fields(S, vol);
+         const double rm = r0 < r1 ? r1 : r0;
+         S.thr_f = (float)((double)L.f_ly_squ * rm * rm * (1.0 + 1e-3) + 1e-3);
+         S.bundle = (int32_t)b;
+         table[at++] = S;
+         cand += count;
       }
    }
    if (plan->segs.size() > 0xFFFFFFF0ull) {
@@ -454,9 +493,15 @@ tissue_write(const unsigned long long *__restrict__ keys,
              float *__restrict__ vec, const unsigned *__restrict__ min_bundle,
              unsigned long long *__restrict__ counters) {
    unsigned long long n_overflow = 0, n_overlap = 0, n_slow = 0;
-   const bool small_index = n_vox < (int64_t(1) << 32);
-   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_vox;
-        i += (int64_t)gridDim.x * blockDim.x) {
+   // one warp per (x, y) row, lanes along z: coalesced, one division per row
+   const int lane = threadIdx.x & 31;
+   const int64_t n_rows = n_vox / Z;
+   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+   for (int64_t row = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); row < n_rows;
+        row += warps) {
+   const int x = (int)(row / Y), y = (int)(row - (row / Y) * Y);
+   for (int z = lane; z < (int)Z; z += 32) {
+      const int64_t i = row * Z + z;
       const unsigned long long key = keys[i];
       if (key == ~0ull) {
          label[i] = 0;
@@ -471,19 +516,6 @@ tissue_write(const unsigned long long *__restrict__ keys,
       const float dist_squ = __uint_as_float((unsigned)(key >> 32));
       const SegDev &S = segs[seg];
       const LayerDev &L = layers[S.bundle];
-      int x, y, z;
-      if (small_index) {
-         const unsigned ii = (unsigned)i, zz = (unsigned)Z, yy = (unsigned)Y;
-         const unsigned xy = ii / zz;
-         z = (int)(ii - xy * zz);
-         x = (int)(xy / yy);
-         y = (int)(xy - (unsigned)x * yy);
-      } else {
-         z = (int)(i % Z);
-         const int64_t xy = i / Z;
-         y = (int)(xy % Y);
-         x = (int)(xy / Y);
-      }
       const float lpt[3] = {(float)(x - S.base[0]) + 0.5f, (float)(y - S.base[1]) + 0.5f,
                             (float)(z - S.base[2]) + 0.5f};
       FastCand fc;
@@ -543,6 +575,7 @@ tissue_write(const unsigned long long *__restrict__ keys,
       vec[3 * i + 0] = o[0];
       vec[3 * i + 1] = o[1];
       vec[3 * i + 2] = o[2];
+   }
    }
    if (n_overlap)
       atomicAdd(&counters[0], n_overlap);
@@ -612,7 +645,8 @@ int run_tissue(const TissuePlan &p, int only_label, int32_t *d_label,
       int dev = 0, sms = 0;
       FPGB_CUDA_TRY(cudaGetDevice(&dev));
       FPGB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-      const int64_t blocks = std::min<int64_t>((nvox + 255) / 256, (int64_t)sms * 16);
+      const int64_t rows = p.X * p.Y;
+      const int64_t blocks = std::min<int64_t>((rows + 7) / 8, (int64_t)sms * 16);
       tissue_write<<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, st>>>(
           keys, segs, layers, p.max_layer, nvox, p.Y, p.Z, d_label,
           only_label ? nullptr : d_vector, minb, counters);

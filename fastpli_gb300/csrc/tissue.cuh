@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <memory>
 #include <vector>
 
 #include "fpgb_common.cuh"
@@ -30,6 +31,7 @@ struct SegDev {
    float pl_hi[3], pl_lo[3]; // p - base
    float v_hi[3], v_lo[3];   // v
    float c2_hi, c2_lo;       // c2
+   float c2_rcp;             // float(1 / c2)
    float r0_hi, r0_lo;       // r0
    float dr_hi, dr_lo;       // r1 - r0
    float rsq0, rsq1;         // float(r^2) at t = 0 and t = 1 (exact)
@@ -53,13 +55,36 @@ struct LayerDev {
    char model[kMaxLayers] = {};
 };
 
+// Growable array without value-initialisation (the segment table is written
+// in full by the planner; zeroing 200+ bytes per segment first is waste).
+template <class T> class RawArray {
+ public:
+   void reset(size_t n) {
+      p_.reset(n ? new T[n] : nullptr);
+      n_ = n;
+   }
+   void clear() { reset(0); }
+   T *data() { return p_.get(); }
+   const T *data() const { return p_.get(); }
+   size_t size() const { return n_; }
+   bool empty() const { return n_ == 0; }
+   T &operator[](size_t i) { return p_[i]; }
+   const T &operator[](size_t i) const { return p_[i]; }
+   const T *begin() const { return p_.get(); }
+   const T *end() const { return p_.get() + n_; }
+
+ private:
+   std::unique_ptr<T[]> p_;
+   size_t n_ = 0;
+};
+
 struct TissuePlan {
    int64_t X = 0, Y = 0, Z = 0;
    int64_t n_bundles = 0;
    int max_layer = 0;
    int64_t single_point = 0; // fibers skipped with a warning
    int64_t candidates = 0;   // sum of clipped box volumes
-   std::vector<SegDev> segs;
+   RawArray<SegDev> segs;
    std::vector<LayerDev> layers;
    std::vector<double> props; // (dn, mu) rows
 };

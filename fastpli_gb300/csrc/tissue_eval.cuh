@@ -82,7 +82,8 @@ struct FastRow {
 FPGB_HD void fast_row(const SegDev &S, float ly, float lz, FastRow &r) {
    r.wy = ff_add_f(ff{-S.pl_hi[1], -S.pl_lo[1]}, ly);
    r.wz = ff_add_f(ff{-S.pl_hi[2], -S.pl_lo[2]}, lz);
-   r.c1yz = ff_add(ff_mul(r.wy, ff{S.v_hi[1], S.v_lo[1]}), ff_mul(r.wz, ff{S.v_hi[2], S.v_lo[2]}));
+   r.c1yz = ff_add_sloppy(ff_mul(r.wy, ff{S.v_hi[1], S.v_lo[1]}),
+                          ff_mul(r.wz, ff{S.v_hi[2], S.v_lo[2]}));
    r.wyz2 = r.wy.hi * r.wy.hi + r.wz.hi * r.wz.hi;
 }
 
@@ -94,7 +95,7 @@ FPGB_HD bool fast_candidate_row(const SegDev &S, float lx, const FastRow &row, F
 #pragma unroll
    for (int i = 0; i < 3; i++)
       v[i] = ff{S.v_hi[i], S.v_lo[i]};
-   const ff c1 = ff_add(ff_mul(w[0], v[0]), row.c1yz);
+   const ff c1 = ff_add_sloppy(ff_mul(w[0], v[0]), row.c1yz);
    const float wn = sqrtf(w[0].hi * w[0].hi + row.wyz2);
    const ff c2{S.c2_hi, S.c2_lo};
    const float vn = sqrtf(S.c2_hi);
@@ -103,7 +104,7 @@ FPGB_HD bool fast_candidate_row(const SegDev &S, float lx, const FastRow &row, F
    if (c1.hi < -ec) {
       branch = 0; // c1 < 0: closest = s0, t = 0 (generator.cpp:483-484)
    } else {
-      const ff dq = ff_sub(c1, c2);
+      const ff dq = ff_sub_sloppy(c1, c2);
       if (dq.hi > ec)
          branch = 1; // c2 <= c1: closest = s1, t = 1 (:487-488)
       else if (c1.hi > ec && dq.hi < -ec)
@@ -122,14 +123,14 @@ FPGB_HD bool fast_candidate_row(const SegDev &S, float lx, const FastRow &row, F
       bmag = 1.f;
 #pragma unroll
       for (int i = 0; i < 3; i++)
-         c.d[i] = ff_sub(v[i], w[i]);
+         c.d[i] = ff_sub_sloppy(v[i], w[i]);
       c.r_sqr = S.rsq1;
    } else {
-      const ff b = ff_div(c1, c2);
+      const ff b = ff_div_rcp(c1, c2, S.c2_rcp);
       bmag = b.hi;
 #pragma unroll
       for (int i = 0; i < 3; i++)
-         c.d[i] = ff_sub(ff_mul(v[i], b), w[i]);
+         c.d[i] = ff_sub_sloppy(ff_mul(v[i], b), w[i]);
       if (!std::isnan(S.rsq_const)) {
          c.r_sqr = S.rsq_const;
       } else { // r = r0 (1 - t) + r1 t  (fiber.cpp:115-120)
@@ -141,7 +142,7 @@ FPGB_HD bool fast_candidate_row(const SegDev &S, float lx, const FastRow &row, F
             return false;
       }
    }
-   const ff D = ff_norm2(c.d);
+   const ff D = ff_norm2_sloppy(c.d);
    c.dn = sqrtf(fmaxf(D.hi, 0.f));
    c.m = wn + vn * bmag + 1.f;
    const float ed = 0x1p-41f * c.m * (c.dn + 0x1p-20f * c.m) +
