@@ -117,6 +117,29 @@ def _peaks():
         return 6800.0, "fallback"
 
 
+def _ncu_traffic(summary):
+    """DRAM bytes (read + write) per launch of the first launch listed in a
+    committed ncu summary under profiles/ (None when absent)."""
+    import re
+    try:
+        text = open(os.path.join(ROOT, "profiles", summary)).read()
+    except OSError:
+        return None
+    unit = {"byte": 1, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9}
+    vals = {}
+    for name in ("dram__bytes_read.sum", "dram__bytes_write.sum"):
+        m = re.search(r"`" + re.escape(name) + r"`\) \| ([0-9.]+) (\w+)", text)
+        if not m:
+            return None
+        vals[name] = float(m.group(1)) * unit.get(m.group(2), 1)
+    return sum(vals.values())
+
+
+# kernels of one device-resident step: the voxelizer's segment binning (count,
+# scan, fill) and brick kernel, then one march per tilt
+VOXELIZER_LAUNCHES = 4
+
+
 def _setup_args(w):
     kw = w.setup_kwargs()
     return (kw["step_size"], kw["light_intensity"], kw["voxel_size"], kw["wavelength"],
@@ -274,20 +297,27 @@ def run_gpu(args):
     hbm_peak, peak_kind = _peaks()
     gen_avg = sum(gen_ms) / len(gen_ms)
     march_avg = sum(march_ms) / len(march_ms)
+    # march: one label (4 B) and one axis (12 B) per ray-voxel step
     march_bytes = 16 * steps_per
     march_gbs = march_bytes / (march_avg * 1e-3) / 1e9
-    # voxelizer algorithmic bytes: key init + key read (8+8) and label/vector
-    # write (16) per voxel
-    gen_bytes = 32 * X * Y * Z
+    # voxelizer: label + vector written once per voxel (16 B); the winner keys
+    # stay in shared memory, the segment table (280 B per segment) is noise
+    gen_bytes = 16 * X * Y * Z
     gen_gbs = gen_bytes / (gen_avg * 1e-3) / 1e9
     if march_avg >= gen_avg:
+        traffic = _ncu_traffic("march_rays_slerp_tilted_crossing512x512x120.md")
         roof = {"kernel": "march_rays (5 tilts)", "bound": "hbm", "achieved": march_gbs,
                 "peak": hbm_peak, "unit": "GB/s", "frac": march_gbs / hbm_peak,
-                "traffic": None, "algorithmic_bytes_per_step": 16, "peak_source": peak_kind}
+                "traffic": traffic, "traffic_per": "one tilted launch (ncu)",
+                "algorithmic_bytes_per_launch": march_bytes / len(w.tilts),
+                "algorithmic_bytes_per_step": 16, "peak_source": peak_kind}
     else:
-        roof = {"kernel": "tissue_keys+tissue_write", "bound": "hbm", "achieved": gen_gbs,
+        traffic = _ncu_traffic("voxel_bricks_crossing512x512x120.md")
+        roof = {"kernel": "voxel_bricks (+ binning)", "bound": "hbm", "achieved": gen_gbs,
                 "peak": hbm_peak, "unit": "GB/s", "frac": gen_gbs / hbm_peak,
-                "traffic": None, "algorithmic_bytes_per_voxel": 32, "peak_source": peak_kind}
+                "traffic": traffic, "traffic_per": "one launch (ncu)",
+                "algorithmic_bytes_per_launch": gen_bytes,
+                "algorithmic_bytes_per_voxel": 16, "peak_source": peak_kind}
 
     line = None
     if rank == 0:
@@ -311,7 +341,7 @@ def run_gpu(args):
             "roofline": roof, "cpu_baseline": cpu,
             "e2e": {"value": ws * steps_per / e2e_s, "unit": UNIT,
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-            "gpu_launches": args.steps * (2 + len(w.tilts)),
+            "gpu_launches": args.steps * (VOXELIZER_LAUNCHES + len(w.tilts)),
             "clocks": clocks.summary(),
         }
         print(json.dumps(line), flush=True)

@@ -8,8 +8,9 @@ Flags that matter for parity:
   * host code: ``-ffp-contract=off`` — the host planning replays the
     reference's double arithmetic (segment boxes, ray geometry) and must not
     fuse multiply-adds (GCC fuses by default on aarch64).
-  * ``tissue.cu``: ``-fmad=false`` — the voxelizer's exact double path must
-    round every product and sum separately, as the reference does.
+  * ``tissue.cu``, ``voxel_bricks.cu``: ``-fmad=false`` — the voxelizer's
+    exact double path must round every product and sum separately, as the
+    reference does.
 """
 
 import concurrent.futures as cf
@@ -29,8 +30,9 @@ LIB_PATH = os.path.join(OUT_DIR, LIB_NAME)
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
           "-I", os.path.join(ROOT, "include")]
-PER_FILE = {"tissue.cu": ["-fmad=false", "-Xcompiler", "-fopenmp"],
-            "batch_tissue.cu": ["-fmad=false"]}
+PER_FILE = {"capi.cu": ["-Xcompiler", "-fopenmp"],
+            "tissue.cu": ["-fmad=false", "-Xcompiler", "-fopenmp"],
+            "voxel_bricks.cu": ["-fmad=false"]}
 
 
 def _nvcc():

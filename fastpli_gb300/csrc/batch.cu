@@ -2,10 +2,9 @@
 // fibers, layers and tilt set, voxelized and marched by one fixed sequence of
 // launches that can be captured once in a CUDA graph and replayed.
 //
-//   batch_keys    the voxelizer key pass over the segments of ALL tiles (one
-//                 CTA per segment, as tissue_keys), each segment writing into
-//                 its tile's slice of one key arena;
-//   batch_write   label/vector for all tiles (grid.y = tile);
+//   voxelizer     the brick voxelizer (voxel_bricks.cu) over the bricks of
+//                 ALL tiles, numbered consecutively; each brick writes its
+//                 tile's labels and vectors;
 //   batch_march   a persistent kernel: CTAs pull work items (tile-tilt pair,
 //                 block of rays) from an atomic counter in cost order until
 //                 the queue is empty, and march them with the same per-ray
@@ -26,7 +25,7 @@
 #include "march_core.cuh"
 #include "raymarch.cuh"
 #include "tissue.cuh"
-#include "batch.cuh"
+#include "voxel_bricks.cuh"
 
 namespace fpgb {
 
@@ -54,10 +53,11 @@ struct fpgb_batch_impl {
    std::vector<size_t> label_off, vector_off, image_off, epa_off;
    size_t arena_bytes = 0;
    // workspace layout (bytes)
-   size_t ws_keys = 0, ws_minb = 0, ws_segs = 0, ws_segtile = 0, ws_layers = 0, ws_tiles = 0,
-          ws_prm = 0, ws_items = 0, ws_tables = 0, ws_counters = 0, ws_bytes = 0;
+   size_t ws_bricks = 0, ws_segs = 0, ws_segtile = 0, ws_layers = 0, ws_tiles = 0, ws_prm = 0,
+          ws_items = 0, ws_tables = 0, ws_counters = 0, ws_bytes = 0;
    std::vector<size_t> table_off; // per pair: lut then ztab, relative to ws_tables
    int64_t total_vox = 0, steps = 0;
+   int64_t n_bricks = 0, brick_pairs = 0;
    bool any_multi_bundle = false;
    int want_epa = 0;
    // bound buffers
@@ -198,6 +198,11 @@ int plan_batch(int64_t n_tiles, const fpgb_volume *vols, const fpgb_fibers *fibe
       TileDev T{};
       T.vox_base = vox;
       T.n_vox = P.X * P.Y * P.Z;
+      T.brick_base = B->n_bricks;
+      int64_t nbr = 0;
+      tile_bricks(P.X, P.Y, P.Z, T.nb, &nbr);
+      B->n_bricks += nbr;
+      B->brick_pairs += P.brick_pairs;
       T.X = (int32_t)P.X;
       T.Y = (int32_t)P.Y;
       T.Z = (int32_t)P.Z;
@@ -282,8 +287,7 @@ int plan_batch(int64_t n_tiles, const fpgb_volume *vols, const fpgb_fibers *fibe
 
    // workspace
    size_t w = 0;
-   B->ws_keys = take(w, sizeof(unsigned long long) * vox);
-   B->ws_minb = B->any_multi_bundle ? take(w, sizeof(unsigned) * vox) : 0;
+   B->ws_bricks = take(w, brick_workspace_bytes(B->n_bricks, B->brick_pairs));
    B->ws_segs = take(w, sizeof(SegDev) * B->segs.size());
    B->ws_segtile = take(w, sizeof(int32_t) * B->seg_tile.size());
    B->ws_layers = take(w, sizeof(LayerDev) * B->layers.size());
@@ -389,8 +393,6 @@ int run_batch(fpgb_batch_impl *B, int march_ctas_per_sm, int chunk, cudaStream_t
       return FPGB_EINVAL;
    }
    char *W = B->ws;
-   auto *keys = reinterpret_cast<unsigned long long *>(W + B->ws_keys);
-   auto *minb = B->any_multi_bundle ? reinterpret_cast<unsigned *>(W + B->ws_minb) : nullptr;
    auto *segs = reinterpret_cast<const SegDev *>(W + B->ws_segs);
    auto *seg_tile = reinterpret_cast<const int32_t *>(W + B->ws_segtile);
    auto *layers = reinterpret_cast<const LayerDev *>(W + B->ws_layers);
@@ -404,19 +406,11 @@ int run_batch(fpgb_batch_impl *B, int march_ctas_per_sm, int chunk, cudaStream_t
    auto *counters = reinterpret_cast<unsigned long long *>(W + B->ws_counters);
    unsigned long long *next = counters + kCounterWords;
 
-   FPGB_CUDA_TRY(cudaMemsetAsync(keys, 0xFF, sizeof(unsigned long long) * B->total_vox, st));
-   if (minb)
-      FPGB_CUDA_TRY(cudaMemsetAsync(minb, 0xFF, sizeof(unsigned) * B->total_vox, st));
    FPGB_CUDA_TRY(cudaMemsetAsync(counters, 0, sizeof(unsigned long long) * (kCounterWords + 2),
                                  st));
-   const int sms = B->sms;
-   {
-      int64_t maxv = 0;
-      for (const TileDev &T : B->tile_dev)
-         maxv = std::max(maxv, T.n_vox);
-      FPGB_TRY(launch_batch_tissue(segs, seg_tile, (int64_t)B->segs.size(), tiles, (int64_t)nt,
-                                   maxv, layers, keys, minb, lptr, vptr, counters, sms, st));
-   }
+   FPGB_TRY(launch_voxel_bricks(segs, seg_tile, (int64_t)B->segs.size(), tiles, (int64_t)nt,
+                                B->n_bricks, B->brick_pairs, layers, B->any_multi_bundle, lptr,
+                                vptr, W + B->ws_bricks, counters, st));
    const int64_t n0 = B->n_untilted, n1 = (int64_t)B->items.size() - B->n_untilted;
    const int ch = chunk > 0 ? chunk : 4;
 #define FPGB_BATCH_MARCH(M)                                                                    \
@@ -540,6 +534,10 @@ int fpgb_batch_warnings(const fpgb_batch *b, fpgb_warnings *w, int64_t *fp64_rep
    if (h[6] & kStatusLabelRange) {
       set_error("batch: label out of range");
       return FPGB_EINVAL;
+   }
+   if (h[6] & kStatusOverflow) { // the device binning disagreed with the host plan
+      set_error("batch: internal error, segment-brick lists overflowed");
+      return FPGB_ECUDA;
    }
    if (w) {
       warnings_from_counters(reinterpret_cast<const long long *>(h), w);

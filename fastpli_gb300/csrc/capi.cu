@@ -1,6 +1,10 @@
-// Library-wide C-ABI helpers: error string, version, cached device pool.
+// Library-wide C-ABI helpers: error string, version, cached device pool,
+// host page pre-faulting.
 #include <cuda_runtime.h>
+#include <omp.h>
+#include <unistd.h>
 
+#include <algorithm>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -71,6 +75,19 @@ int pool_get(int slot, size_t bytes, void **ptr, cudaStream_t stream) {
    }
    *ptr = e.ptr;
    return FPGB_OK;
+}
+
+void prefault_host(void *p, size_t bytes) {
+   if (!p || bytes < (size_t(8) << 20))
+      return;
+   const int64_t pg = (int64_t)sysconf(_SC_PAGESIZE);
+   if (pg <= 0)
+      return;
+   volatile char *c = static_cast<volatile char *>(p);
+   const int64_t n = ((int64_t)bytes + pg - 1) / pg;
+#pragma omp parallel for schedule(static) num_threads(std::min(16, omp_get_max_threads()))
+   for (int64_t i = 0; i < n; i++)
+      c[i * pg] = 0;
 }
 
 int pool_release_all() {

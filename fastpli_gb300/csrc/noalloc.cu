@@ -1,9 +1,8 @@
 // Voxelizer entry point that allocates no device memory.
 //
 // The regular device entry point (fpgb_generate_tissue_device) needs a
-// scratch workspace: 8 bytes per voxel of distance/segment keys, 4 more per
-// voxel when several bundles are voxelized, plus the segment and layer
-// tables.  It takes that workspace from the caller or from the library's own
+// scratch workspace: the segment and layer tables and the segment lists of
+// the voxel bricks (the per-voxel keys live in shared memory).  It takes that workspace from the caller or from the library's own
 // cudaMalloc'ed pool.  Some callers can do neither: applications whose
 // device memory is already owned by another allocator (a framework that has
 // reserved the GPU for its caching allocator, a host that budgets HBM per
@@ -19,7 +18,7 @@
 //     before any stream capture;
 //   * every call on a device shares the same array and the array keeps the
 //     previous call's contents; each call re-initialises the parts it reads
-//     (keys, per-voxel bundle minima, counters) before use;
+//     (tables, brick counts and lists, counters) before use;
 //   * calls whose device work overlaps (different streams, or host threads
 //     without ordering) race on the array: serialise them;
 //   * problems whose scratch exceeds the array are rejected with

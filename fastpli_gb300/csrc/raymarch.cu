@@ -538,6 +538,7 @@ int fpgb_run_simulation(const fpgb_setup *setup, const int64_t *dim, const int32
    FPGB_TRY(pool_get(kSlotVector, sizeof(float) * 3 * nvox, &d_vec));
    FPGB_TRY(pool_get(kSlotImage, sizeof(double) * npix * setup->n_rho, &d_img));
    cudaStream_t st = nullptr;
+   prefault_host(image, sizeof(double) * npix * setup->n_rho);
    FPGB_CUDA_TRY(cudaMemcpyAsync(d_label, label, sizeof(int32_t) * nvox,
                                  cudaMemcpyHostToDevice, st));
    FPGB_CUDA_TRY(cudaMemcpyAsync(d_vec, vector, sizeof(float) * 3 * nvox,

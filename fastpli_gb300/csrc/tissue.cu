@@ -7,15 +7,17 @@
 // smallest float distance and, among equal distances, the LAST one in
 // processing order.  Here every (segment, voxel) candidate is independent:
 //
-//   pass 1  tissue_keys   one CTA per segment sweeps the segment's clipped
-//                         bounding box; a cheap FP32 test rejects voxels
-//                         clearly outside the outermost layer, survivors get
-//                         the exact double->float distance of the reference
-//                         and an atomicMin on the 64-bit key
-//                         (float bits of dist_squ) << 32 | (0xFFFFFFFF - seg),
-//                         i.e. smallest distance, then largest segment index.
-//   pass 2  tissue_write  one thread per voxel decodes the winner and
-//                         recomputes its layer and orientation exactly.
+//   binning       every segment's clipped bounding box is binned to the
+//                 8 x 8 x 32 voxel bricks it overlaps;
+//   voxel_bricks  one CTA per brick keeps the brick's 64-bit keys
+//                 (float bits of dist_squ) << 32 | (0xFFFFFFFF - seg), i.e.
+//                 smallest distance, then largest segment index, in shared
+//                 memory: a first sweep stores FP32 upper bounds of the
+//                 candidates certainly inside, a second the exact
+//                 double->float distance of the reference for every
+//                 candidate that can still win; then it decodes each
+//                 voxel's winner and writes its label and orientation
+//                 (voxel_bricks.cu).
 //
 // This translation unit is compiled with -fmad=false: the label and vector
 // decisions depend on separately rounded double products and sums
@@ -33,6 +35,7 @@
 #include "fpgb_common.cuh"
 #include "tissue.cuh"
 #include "tissue_eval.cuh"
+#include "voxel_bricks.cuh"
 
 namespace fpgb {
 
@@ -357,8 +360,8 @@ int plan_tissue(const fpgb_volume *vol, const fpgb_fibers *fb, TissuePlan *plan)
    }
    plan->segs.reset((size_t)fiber_segs[nf]);
    SegDev *table = plan->segs.data();
-   int64_t cand = 0;
-#pragma omp parallel for schedule(dynamic, 32) reduction(+ : cand)
+   int64_t cand = 0, pairs = 0;
+#pragma omp parallel for schedule(dynamic, 32) reduction(+ : cand, pairs)
    for (int64_t fi = 0; fi < nf; fi++) {
       if (!fiber_used(fi))
          continue;
@@ -396,9 +399,18 @@ int plan_tissue(const fpgb_volume *vol, const fpgb_fibers *fb, TissuePlan *plan)
          fill_fast_fields(S, vol);
          const double rm = r0 < r1 ? r1 : r0;
          S.thr_f = (float)((double)L.f_ly_squ * rm * rm * (1.0 + 1e-3) + 1e-3);
+         {
+            const double rn = r0 < r1 ? r0 : r1;
+            const double a = (double)L.f_ly_squ * rn * rn * (1.0 - 1e-5);
+            float af = (float)a;
+            if ((double)af > a)
+               af = std::nextafter(af, 0.f);
+            S.acc_f = af > 0.f ? af : -1.f;
+         }
          S.bundle = (int32_t)b;
          table[at++] = S;
          cand += count;
+         pairs += segment_brick_pairs(S);
       }
    }
    if (plan->segs.size() > 0xFFFFFFF0ull) {
@@ -406,6 +418,7 @@ int plan_tissue(const fpgb_volume *vol, const fpgb_fibers *fb, TissuePlan *plan)
       return FPGB_EINVAL;
    }
    plan->candidates = cand;
+   plan->brick_pairs = pairs;
    return FPGB_OK;
 }
 
@@ -413,196 +426,32 @@ int plan_tissue(const fpgb_volume *vol, const fpgb_fibers *fb, TissuePlan *plan)
 // device code
 // ======================================================================
 
-__global__ void __launch_bounds__(128)
-tissue_keys(const SegDev *__restrict__ segs, int64_t n_segs,
-            const LayerDev *__restrict__ layers, int64_t Y, int64_t Z,
-            unsigned long long *__restrict__ keys,
-            unsigned *__restrict__ min_bundle, unsigned long long *__restrict__ counters) {
-   unsigned long long n_slow = 0;
-   for (int64_t s = blockIdx.x; s < n_segs; s += gridDim.x) {
-      const SegDev &S = segs[s];
-      const float f_ly = layers[S.bundle].f_ly_squ;
-      const int ex = S.ext[0], ey = S.ext[1], ez = S.ext[2];
-      const int plane = ey * ez;
-      const unsigned long long inv_idx =
-          (unsigned long long)(0xFFFFFFFFu - (unsigned)s);
-      const float vfx = S.vf[0], vfy = S.vf[1], vfz = S.vf[2];
-      const float c2f = S.c2f;
-      const bool fast_ok = S.pscale < 0x1p22f;
-      for (int pl = threadIdx.x; pl < plane; pl += blockDim.x) {
-         const int iy = pl / ez, iz = pl - (pl / ez) * ez;
-         const int y = S.lo[1] + iy, z = S.lo[2] + iz;
-         // segment-local voxel centre, exact in float
-         const float ly = (float)(y - S.base[1]) + 0.5f;
-         const float lz = (float)(z - S.base[2]) + 0.5f;
-         // FP32 prefilter
-         const float wy = ly - S.pf[1];
-         const float wz = lz - S.pf[2];
-         FastRow row;
-         if (fast_ok)
-            fast_row(S, ly, lz, row);
-         for (int ix = 0; ix < ex; ix++) {
-            const int x = S.lo[0] + ix;
-            const float lx = (float)(x - S.base[0]) + 0.5f;
-            const float wx = lx - S.pf[0];
-            const float c1f = wx * vfx + wy * vfy + wz * vfz;
-            const float w2 = wx * wx + wy * wy + wz * wz;
-            float d2f;
-            if (c1f <= 0.f) {
-               d2f = w2;
-            } else if (c1f >= c2f) {
-               const float ux = wx - vfx, uy = wy - vfy, uz = wz - vfz;
-               d2f = ux * ux + uy * uy + uz * uz;
-            } else {
-               d2f = w2 - c1f * (c1f / c2f);
-            }
-            const float margin = 1e-4f + 3.8e-6f * (w2 + c2f);
-            if (d2f - margin > S.thr_f)
-               continue;
-            float dist_squ, r_sqr;
-            FastCand fc;
-            if (fast_ok && fast_candidate_row(S, lx, row, fc)) {
-               dist_squ = fc.dist_squ;
-               r_sqr = fc.r_sqr;
-            } else { // exact reference arithmetic
-               const double pt[3] = {(double)x + 0.5, (double)y + 0.5, (double)z + 0.5};
-               double cl[3];
-               exact_dist(S, pt, cl, dist_squ, r_sqr);
-               n_slow++;
-            }
-            if (dist_squ > f_ly * r_sqr) // generator.cpp:329-331
-               continue;
-            const int64_t ind = ((int64_t)x * Y + y) * Z + z;
-            const unsigned long long key =
-                ((unsigned long long)__float_as_uint(dist_squ) << 32) | inv_idx;
-            atomicMin(&keys[ind], key);
-            if (min_bundle)
-               atomicMin(&min_bundle[ind], (unsigned)S.bundle);
-         }
-      }
-   }
-   if (n_slow)
-      atomicAdd(&counters[9], n_slow);
-}
-
-__global__ void __launch_bounds__(256, 3)
-tissue_write(const unsigned long long *__restrict__ keys,
-             const SegDev *__restrict__ segs,
-             const LayerDev *__restrict__ layers, int max_layer, int64_t n_vox,
-             int64_t Y, int64_t Z, int32_t *__restrict__ label,
-             float *__restrict__ vec, const unsigned *__restrict__ min_bundle,
-             unsigned long long *__restrict__ counters) {
-   unsigned long long n_overflow = 0, n_overlap = 0, n_slow = 0;
-   // one warp per (x, y) row, lanes along z: coalesced, one division per row
-   const int lane = threadIdx.x & 31;
-   const int64_t n_rows = n_vox / Z;
-   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-   for (int64_t row = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); row < n_rows;
-        row += warps) {
-   const int x = (int)(row / Y), y = (int)(row - (row / Y) * Y);
-   for (int z = lane; z < (int)Z; z += 32) {
-      const int64_t i = row * Z + z;
-      const unsigned long long key = keys[i];
-      if (key == ~0ull) {
-         label[i] = 0;
-         if (vec) {
-            vec[3 * i + 0] = 0.f;
-            vec[3 * i + 1] = 0.f;
-            vec[3 * i + 2] = 0.f;
-         }
-         continue;
-      }
-      const unsigned seg = 0xFFFFFFFFu - (unsigned)(key & 0xFFFFFFFFull);
-      const float dist_squ = __uint_as_float((unsigned)(key >> 32));
-      const SegDev &S = segs[seg];
-      const LayerDev &L = layers[S.bundle];
-      const float lpt[3] = {(float)(x - S.base[0]) + 0.5f, (float)(y - S.base[1]) + 0.5f,
-                            (float)(z - S.base[2]) + 0.5f};
-      FastCand fc;
-      bool fast = S.pscale < 0x1p22f && fast_candidate(S, lpt, fc);
-      float r_sqr = fc.r_sqr;
-      double cl[3];
-      if (!fast) {
-         const double pt[3] = {(double)x + 0.5, (double)y + 0.5, (double)z + 0.5};
-         float d_chk;
-         exact_dist(S, pt, cl, d_chk, r_sqr);
-      }
-      // std::lower_bound(scale^2, double(dist_squ / r_sqr)) (generator.cpp:345-349)
-      const float qv = dist_squ / r_sqr;
-      int ly = 0;
-      while (ly < L.n && qv > L.sq_fdown[ly])
-         ly++;
-      label[i] = ly + 1 + S.bundle * max_layer;
-      if (min_bundle && min_bundle[i] < (unsigned)S.bundle)
-         n_overlap++;
-      char m = 'b';
-      if (ly < L.n)
-         m = L.model[ly];
-      else
-         n_overflow++;
-      if (!vec)
-         continue;
-      float o[3] = {0.f, 0.f, 0.f};
-      if (m == 'p') {
-         o[0] = S.vp[0];
-         o[1] = S.vp[1];
-         o[2] = S.vp[2];
-      } else if (m == 'r') {
-         if (!(fast && fast_radial(S, fc, o))) {
-            const double pt[3] = {(double)x + 0.5, (double)y + 0.5, (double)z + 0.5};
-            if (fast) {
-               float d_chk, r_chk;
-               exact_dist(S, pt, cl, d_chk, r_chk);
-            }
-            n_slow++;
-            // vm::unit(point - closest) in the reference's double order
-            double nv[3] = {pt[0] - cl[0], pt[1] - cl[1], pt[2] - cl[2]};
-            double n2 = 0.0;
-            n2 = n2 + nv[0] * nv[0];
-            n2 = n2 + nv[1] * nv[1];
-            n2 = n2 + nv[2] * nv[2];
-            if (n2 > 0) {
-               const double inv = 1.0 / sqrt(n2);
-               nv[0] = nv[0] * inv;
-               nv[1] = nv[1] * inv;
-               nv[2] = nv[2] * inv;
-            }
-            o[0] = (float)nv[0];
-            o[1] = (float)nv[1];
-            o[2] = (float)nv[2];
-         }
-      }
-      vec[3 * i + 0] = o[0];
-      vec[3 * i + 1] = o[1];
-      vec[3 * i + 2] = o[2];
-   }
-   }
-   if (n_overlap)
-      atomicAdd(&counters[0], n_overlap);
-   if (n_overflow)
-      atomicAdd(&counters[5], n_overflow);
-   if (n_slow)
-      atomicAdd(&counters[9], n_slow);
-}
-
 // ======================================================================
 // launch
 // ======================================================================
+// Device workspace of one voxelization: the tile header (one TileDev and the
+// label / vector pointers), segment table, layers, counters, and the brick
+// lists of the voxelizer.
+static int64_t plan_bricks(const TissuePlan &p, int32_t nb[3]) {
+   int64_t n = 0;
+   tile_bricks(p.X, p.Y, p.Z, nb, &n);
+   return n;
+}
+
 size_t tissue_workspace_bytes(const TissuePlan &p) {
-   const int64_t nvox = p.X * p.Y * p.Z;
-   size_t b = align_up(sizeof(unsigned long long) * nvox, 256);
-   if (p.n_bundles > 1)
-      b += align_up(sizeof(unsigned) * nvox, 256);
+   int32_t nb[3];
+   const int64_t n_bricks = plan_bricks(p, nb);
+   size_t b = align_up(sizeof(TileDev) + 2 * sizeof(void *), 256);
    b += align_up(sizeof(SegDev) * std::max<size_t>(p.segs.size(), 1), 256);
    b += align_up(sizeof(LayerDev) * p.layers.size(), 256);
    b += align_up(sizeof(unsigned long long) * kCounterWords, 256);
+   b += brick_workspace_bytes(n_bricks, p.brick_pairs);
    return b;
 }
 
 int run_tissue(const TissuePlan &p, int only_label, int32_t *d_label,
                float *d_vector, void *d_ws, size_t ws_bytes,
                unsigned long long **d_counters_out, cudaStream_t st) {
-   const int64_t nvox = p.X * p.Y * p.Z;
    const size_t need = tissue_workspace_bytes(p);
    if (ws_bytes < need) {
       set_error("generate_tissue: workspace %zu bytes < %zu needed", ws_bytes, need);
@@ -612,46 +461,49 @@ int run_tissue(const TissuePlan &p, int only_label, int32_t *d_label,
       set_error("generate_tissue: workspace must be 256-byte aligned");
       return FPGB_EINVAL;
    }
+   int32_t nb[3];
+   const int64_t n_bricks = plan_bricks(p, nb);
    char *w = static_cast<char *>(d_ws);
-   auto *keys = reinterpret_cast<unsigned long long *>(w);
-   w += align_up(sizeof(unsigned long long) * nvox, 256);
-   unsigned *minb = nullptr;
-   if (p.n_bundles > 1) {
-      minb = reinterpret_cast<unsigned *>(w);
-      w += align_up(sizeof(unsigned) * nvox, 256);
-   }
+   char *head = w;
+   w += align_up(sizeof(TileDev) + 2 * sizeof(void *), 256);
    auto *segs = reinterpret_cast<SegDev *>(w);
    w += align_up(sizeof(SegDev) * std::max<size_t>(p.segs.size(), 1), 256);
    auto *layers = reinterpret_cast<LayerDev *>(w);
    w += align_up(sizeof(LayerDev) * p.layers.size(), 256);
    auto *counters = reinterpret_cast<unsigned long long *>(w);
+   w += align_up(sizeof(unsigned long long) * kCounterWords, 256);
 
-   FPGB_CUDA_TRY(cudaMemsetAsync(keys, 0xFF, sizeof(unsigned long long) * nvox, st));
-   if (minb)
-      FPGB_CUDA_TRY(cudaMemsetAsync(minb, 0xFF, sizeof(unsigned) * nvox, st));
+   // the single volume as tile 0 of the brick voxelizer
+   struct {
+      TileDev t;
+      void *label, *vector;
+   } h{};
+   h.t.vox_base = 0;
+   h.t.n_vox = p.X * p.Y * p.Z;
+   h.t.brick_base = 0;
+   h.t.X = (int32_t)p.X;
+   h.t.Y = (int32_t)p.Y;
+   h.t.Z = (int32_t)p.Z;
+   h.t.max_layer = p.max_layer;
+   h.t.layer_base = 0;
+   for (int i = 0; i < 3; i++)
+      h.t.nb[i] = nb[i];
+   h.label = d_label;
+   h.vector = only_label ? nullptr : d_vector;
+   static_assert(sizeof(h) == sizeof(TileDev) + 2 * sizeof(void *), "tile header layout");
+
    FPGB_CUDA_TRY(cudaMemsetAsync(counters, 0, sizeof(unsigned long long) * kCounterWords, st));
+   FPGB_CUDA_TRY(cudaMemcpyAsync(head, &h, sizeof(h), cudaMemcpyHostToDevice, st));
    if (!p.segs.empty())
       FPGB_CUDA_TRY(cudaMemcpyAsync(segs, p.segs.data(), sizeof(SegDev) * p.segs.size(),
                                     cudaMemcpyHostToDevice, st));
    FPGB_CUDA_TRY(cudaMemcpyAsync(layers, p.layers.data(), sizeof(LayerDev) * p.layers.size(),
                                  cudaMemcpyHostToDevice, st));
-   if (!p.segs.empty()) {
-      const int64_t n = (int64_t)p.segs.size();
-      const unsigned grid = (unsigned)std::min<int64_t>(n, 1 << 30);
-      tissue_keys<<<grid, 128, 0, st>>>(segs, n, layers, p.Y, p.Z, keys, minb, counters);
-      FPGB_CUDA_TRY(cudaGetLastError());
-   }
-   {
-      int dev = 0, sms = 0;
-      FPGB_CUDA_TRY(cudaGetDevice(&dev));
-      FPGB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-      const int64_t rows = p.X * p.Y;
-      const int64_t blocks = std::min<int64_t>((rows + 7) / 8, (int64_t)sms * 16);
-      tissue_write<<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, st>>>(
-          keys, segs, layers, p.max_layer, nvox, p.Y, p.Z, d_label,
-          only_label ? nullptr : d_vector, minb, counters);
-      FPGB_CUDA_TRY(cudaGetLastError());
-   }
+   auto *tile = reinterpret_cast<const TileDev *>(head);
+   auto *lp = reinterpret_cast<int32_t *const *>(head + sizeof(TileDev));
+   auto *vp = reinterpret_cast<float *const *>(head + sizeof(TileDev) + sizeof(void *));
+   FPGB_TRY(launch_voxel_bricks(segs, nullptr, (int64_t)p.segs.size(), tile, 1, n_bricks,
+                                p.brick_pairs, layers, p.n_bundles > 1, lp, vp, w, counters, st));
    if (d_counters_out)
       *d_counters_out = counters;
    return FPGB_OK;
@@ -679,6 +531,10 @@ static int read_tissue_warnings(const TissuePlan &p, unsigned long long *d_count
    long long h[kCounterWords];
    FPGB_CUDA_TRY(cudaMemcpyAsync(h, d_counters, sizeof h, cudaMemcpyDeviceToHost, st));
    FPGB_CUDA_TRY(cudaStreamSynchronize(st));
+   if (h[6] & kStatusOverflow) { // the device binning disagreed with the host plan
+      set_error("generate_tissue: internal error, segment-brick lists overflowed");
+      return FPGB_ECUDA;
+   }
    warnings_from_counters(h, w);
    w->overlap = w->overlap > 0 ? 1 : 0; // the reference warns once (generator.cpp:353-359)
    w->single_point = p.single_point;
@@ -742,6 +598,10 @@ int fpgb_generate_tissue(const fpgb_volume *vol, const fpgb_fibers *fibers, int 
    unsigned long long *d_counters = nullptr;
    FPGB_TRY(run_tissue(p, only_label, (int32_t *)d_label, (float *)d_vec, d_ws, need,
                        &d_counters, st));
+   // while the voxelizer runs
+   prefault_host(label, sizeof(int32_t) * nvox);
+   if (!only_label)
+      prefault_host(vector, sizeof(float) * 3 * nvox);
    FPGB_CUDA_TRY(cudaMemcpyAsync(label, d_label, sizeof(int32_t) * nvox,
                                  cudaMemcpyDeviceToHost, st));
    if (!only_label)

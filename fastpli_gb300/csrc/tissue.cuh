@@ -23,6 +23,8 @@ struct SegDev {
    float vf[3];   // float(v)
    float c2f;     // float(c2)
    float thr_f;   // prefilter bound on dist^2 (>= f_ly_squ * max(r0,r1)^2)
+   float acc_f;   // dist^2 at or below which a candidate is certainly inside
+                  // (<= f_ly_squ * min(r0,r1)^2, rounded down)
    int32_t base[3]; // floor(p)
    int32_t lo[3];   // clipped box start (generator.cpp:304)
    int32_t ext[3];  // clipped box extent
@@ -84,6 +86,7 @@ struct TissuePlan {
    int max_layer = 0;
    int64_t single_point = 0; // fibers skipped with a warning
    int64_t candidates = 0;   // sum of clipped box volumes
+   int64_t brick_pairs = 0;  // (segment, brick) pairs of the brick voxelizer
    RawArray<SegDev> segs;
    std::vector<LayerDev> layers;
    std::vector<double> props; // (dn, mu) rows

@@ -39,6 +39,31 @@ FPGB_HD void closest_point(const SegDev &S, const double pt[3],
    }
 }
 
+// FP32 estimate of a candidate's dist^2 from segment-local inputs (w = voxel
+// centre - float(p - base), float(v), float(c2), float(1 / c2)), and a
+// bound: the float that
+// the reference's double arithmetic produces (exact_dist) lies in
+// [d2f - margin, d2f + margin].  The bound covers the rounding of the float
+// inputs, of every FP32 operation, of the branch decision (the distance is
+// continuous across the branches) and of the reference's own final rounding;
+// a host build checks it over every voxel of random segment boxes.
+FPGB_HD float approx_dist2(float wx, float wy, float wz, float vx, float vy, float vz,
+                           float c2f, float rc2, float &margin) {
+   const float c1f = wx * vx + wy * vy + wz * vz;
+   const float w2 = wx * wx + wy * wy + wz * wz;
+   float d2f;
+   if (c1f <= 0.f) {
+      d2f = w2;
+   } else if (c1f >= c2f) {
+      const float ux = wx - vx, uy = wy - vy, uz = wz - vz;
+      d2f = ux * ux + uy * uy + uz * uz;
+   } else {
+      d2f = w2 - c1f * (c1f * rc2);
+   }
+   margin = 1e-4f + 3.8e-6f * (w2 + c2f);
+   return d2f;
+}
+
 // float(|cl - pt|^2) and float(r(t)^2) exactly as generator.cpp:327-328.
 FPGB_HD void exact_dist(const SegDev &S, const double pt[3],
                                            double cl[3], float &dist_squ,

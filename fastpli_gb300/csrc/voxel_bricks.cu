@@ -1,0 +1,573 @@
+// Brick-tiled voxelizer (declarations and overview in voxel_bricks.cuh).
+//
+// Compiled with -fmad=false: the FP64 replay of the reference arithmetic
+// (tissue_eval.cuh) must round every product and sum separately, and the
+// FP32 estimate of the key passes must be the same in both passes.
+//
+// Winner keys.  A voxel's key is float_bits(dist^2) << 32 |
+// (0xFFFFFFFF - segment): the minimum over every accepted (segment, voxel)
+// candidate is the smallest distance, ties going to the LAST segment, which
+// is the reference's `>=` overwrite rule (generator.cpp:329-340).  Keys live
+// in shared memory for the lifetime of the brick's CTA and are minimised
+// with shared-memory atomics.
+//
+// Two key passes over the brick's segments:
+//
+//   BOUND  every candidate that is certainly accepted (FP32 estimate plus its
+//          bound at or below f_ly_squ * min(r0, r1)^2) stores an upper bound
+//          ub of its exact dist^2 as the key ub << 32 | 0xFFFFFFFF, and its
+//          bundle in the bundle minimum;
+//   EXACT  a candidate whose lower bound exceeds the voxel's current key
+//          cannot be the minimum and is skipped; the rest are evaluated with
+//          the reference's arithmetic (two-float fast path, FP64 replay) and
+//          stored as exact keys.
+//
+// The true winner w (smallest exact dist^2 among accepted candidates, last
+// segment on ties) is never skipped: every stored value is >= its distance
+// (an upper bound belongs to an accepted candidate, whose exact distance is
+// >= w's), and w's lower bound is <= its own distance.  Candidates tied with
+// w are not skipped either, so the tie rule holds.  An upper-bound key is
+// >= w's exact key (equal only when w is segment 0: the same value), so the
+// final key is w's, bit for bit.  A candidate that the bound filter skips
+// but that was not certainly accepted is still decided exactly when the
+// bundle minimum is kept (multi-bundle volumes), so that stays exact too.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "ff.cuh"
+#include "fpgb_common.cuh"
+#include "tissue.cuh"
+#include "tissue_eval.cuh"
+#include "voxel_bricks.cuh"
+
+namespace fpgb {
+
+constexpr int kBrickThreads = 256;
+constexpr int kBrickWarps = kBrickThreads / 32;
+static_assert(kBrickZ == 32, "the write phase maps one lane to one z of a brick row");
+
+void tile_bricks(int64_t X, int64_t Y, int64_t Z, int32_t nb[3], int64_t *n_bricks) {
+   nb[0] = (int32_t)((X + kBrickX - 1) / kBrickX);
+   nb[1] = (int32_t)((Y + kBrickY - 1) / kBrickY);
+   nb[2] = (int32_t)((Z + kBrickZ - 1) / kBrickZ);
+   *n_bricks = (int64_t)nb[0] * nb[1] * nb[2];
+}
+
+FPGB_HD int64_t brick_range(int lo, int ext, int b, int &b0) {
+   b0 = lo / b;
+   return ext > 0 ? (lo + ext - 1) / b - b0 + 1 : 0;
+}
+
+int64_t segment_brick_pairs(const SegDev &S) {
+   int b0;
+   return brick_range(S.lo[0], S.ext[0], kBrickX, b0) * brick_range(S.lo[1], S.ext[1], kBrickY, b0) *
+          brick_range(S.lo[2], S.ext[2], kBrickZ, b0);
+}
+
+size_t brick_workspace_bytes(int64_t n_bricks, int64_t n_pairs) {
+   size_t w = 0;
+   w += align_up(sizeof(unsigned) * (n_bricks + 1), 256); // offsets
+   w += align_up(sizeof(unsigned) * std::max<int64_t>(n_bricks, 1), 256); // counts, then cursors
+   w += align_up(sizeof(unsigned) * std::max<int64_t>(n_pairs, 1), 256);  // segment lists
+   return w;
+}
+
+// ---------------------------------------------------------------- binning ---
+template <bool FILL>
+__global__ void brick_bin(const SegDev *__restrict__ segs, const int32_t *__restrict__ seg_tile,
+                          int64_t n_segs, const TileDev *__restrict__ tiles,
+                          unsigned *__restrict__ counts, const unsigned *__restrict__ offsets,
+                          unsigned *__restrict__ list, int64_t n_pairs,
+                          unsigned long long *__restrict__ counters) {
+   for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n_segs;
+        s += (int64_t)gridDim.x * blockDim.x) {
+      const SegDev &S = segs[s];
+      const TileDev &T = tiles[seg_tile ? seg_tile[s] : 0];
+      int bx0, by0, bz0;
+      const int64_t nx = brick_range(S.lo[0], S.ext[0], kBrickX, bx0);
+      const int64_t ny = brick_range(S.lo[1], S.ext[1], kBrickY, by0);
+      const int64_t nz = brick_range(S.lo[2], S.ext[2], kBrickZ, bz0);
+      for (int64_t i = 0; i < nx; i++)
+         for (int64_t j = 0; j < ny; j++)
+            for (int64_t k = 0; k < nz; k++) {
+               const int64_t b =
+                   T.brick_base + ((bx0 + i) * T.nb[1] + (by0 + j)) * T.nb[2] + (bz0 + k);
+               const unsigned slot = atomicAdd(&counts[b], 1u);
+               if (FILL) {
+                  const int64_t at = (int64_t)offsets[b] + slot;
+                  if (at < offsets[b + 1] && at < n_pairs)
+                     list[at] = (unsigned)s;
+                  else
+                     atomicOr(&counters[6], (unsigned long long)kStatusOverflow);
+               }
+            }
+   }
+}
+
+// Exclusive scan of the per-brick counts (one CTA; each thread scans a
+// contiguous chunk, the chunk sums are scanned across the block).
+__global__ void __launch_bounds__(1024)
+brick_scan(const unsigned *__restrict__ counts, int64_t n, unsigned *__restrict__ offsets,
+           unsigned long long *__restrict__ counters) {
+   __shared__ unsigned long long part[1024];
+   const int t = threadIdx.x;
+   const int64_t per = (n + blockDim.x - 1) / blockDim.x;
+   const int64_t a = n < t * per ? n : t * per, b = n < a + per ? n : a + per;
+   unsigned long long sum = 0;
+   for (int64_t i = a; i < b; i++)
+      sum += counts[i];
+   part[t] = sum;
+   __syncthreads();
+   for (int d = 1; d < (int)blockDim.x; d <<= 1) { // Hillis-Steele inclusive scan
+      const unsigned long long v = t >= d ? part[t - d] : 0ull;
+      __syncthreads();
+      part[t] += v;
+      __syncthreads();
+   }
+   unsigned long long run = part[t] - sum;
+   for (int64_t i = a; i < b; i++) {
+      offsets[i] = (unsigned)run;
+      run += counts[i];
+   }
+   if (t == (int)blockDim.x - 1) {
+      offsets[n] = (unsigned)part[t];
+      if (part[t] >= 0xFFFFFFFFull)
+         atomicOr(&counters[6], (unsigned long long)kStatusOverflow);
+   }
+}
+
+// ------------------------------------------------------------ key passes ---
+// The part of segment S's clipped box inside the brick (origin o, extent n),
+// walked by a warp 32 voxels at a time in a flattened (x, y, z) order.
+struct SubBox {
+   int x0, y0, z0, ey, ez, n;
+   float inv_ez, inv_eyz; // 1/ez, 1/(ey*ez) for division-free index splits
+};
+
+__device__ __forceinline__ bool sub_box(const SegDev &S, int ox, int oy, int oz, int nx, int ny,
+                                        int nz, SubBox &b) {
+   b.x0 = max(S.lo[0], ox);
+   b.y0 = max(S.lo[1], oy);
+   b.z0 = max(S.lo[2], oz);
+   const int ex = min(S.lo[0] + S.ext[0], ox + nx) - b.x0;
+   b.ey = min(S.lo[1] + S.ext[1], oy + ny) - b.y0;
+   b.ez = min(S.lo[2] + S.ext[2], oz + nz) - b.z0;
+   if (ex <= 0 || b.ey <= 0 || b.ez <= 0)
+      return false;
+   b.n = ex * b.ey * b.ez;
+   b.inv_ez = 1.f / (float)b.ez;
+   b.inv_eyz = 1.f / (float)(b.ey * b.ez);
+   return true;
+}
+
+// k-th voxel of the sub-box.  (k + 1/2) / e lies at least 1/(2e) >= 2^-9
+// from an integer for k < 2048 and e <= 256, far beyond the float error of
+// the product, so the truncations are the exact integer quotients.
+__device__ __forceinline__ void sub_box_voxel(const SubBox &b, int k, int &x, int &y, int &z) {
+   const int ix = (int)(((float)k + 0.5f) * b.inv_eyz);
+   const int r = k - ix * (b.ey * b.ez);
+   const int iy = (int)(((float)r + 0.5f) * b.inv_ez);
+   x = b.x0 + ix;
+   y = b.y0 + iy;
+   z = b.z0 + (r - iy * b.ez);
+}
+
+__device__ __forceinline__ int brick_index(int x, int y, int z, int ox, int oy, int oz) {
+   return ((x - ox) * kBrickY + (y - oy)) * kBrickZ + (z - oz);
+}
+
+// Per-segment inputs of the FP32 estimate, held in registers over a sweep.
+struct SegFP32 {
+   float pfx, pfy, pfz, vx, vy, vz, c2f, rc2, thr, acc;
+   int bx, by, bz;
+};
+
+__device__ __forceinline__ SegFP32 seg_fp32(const SegDev &S) {
+   return SegFP32{S.pf[0], S.pf[1], S.pf[2], S.vf[0], S.vf[1], S.vf[2], S.c2f,
+                  S.c2_rcp, S.thr_f, S.acc_f, S.base[0], S.base[1], S.base[2]};
+}
+
+// FP32 estimate of the candidate (segment, voxel x y z): its dist^2 lies in
+// [lo, hi] (directed rounding of estimate -/+ bound).
+__device__ __forceinline__ void candidate_bounds(const SegFP32 &g, int x, int y, int z, float &lo,
+                                                 float &hi) {
+   float mg;
+   const float d2f = approx_dist2((float)(x - g.bx) + 0.5f - g.pfx, (float)(y - g.by) + 0.5f - g.pfy,
+                                  (float)(z - g.bz) + 0.5f - g.pfz, g.vx, g.vy, g.vz, g.c2f, g.rc2,
+                                  mg);
+   lo = __fsub_rd(d2f, mg);
+   hi = __fadd_ru(d2f, mg);
+}
+
+// BOUND pass of one segment over its sub-box.
+template <bool MULTI>
+__device__ __forceinline__ void brick_bound(const SegDev &S, const SubBox &b, int ox, int oy,
+                                            int oz, unsigned long long *skey, unsigned *sminb,
+                                            int lane) {
+   const SegFP32 g = seg_fp32(S);
+   const unsigned bundle = (unsigned)S.bundle;
+   for (int k = lane; k < b.n; k += 32) {
+      int x, y, z;
+      sub_box_voxel(b, k, x, y, z);
+      float lo, hi;
+      candidate_bounds(g, x, y, z, lo, hi);
+      if (!(hi <= g.acc))
+         continue;
+      const int li = brick_index(x, y, z, ox, oy, oz);
+      atomicMin(&skey[li], ((unsigned long long)__float_as_uint(hi) << 32) | 0xFFFFFFFFull);
+      if (MULTI)
+         atomicMin(&sminb[li], bundle);
+   }
+}
+
+// Queue entry flags (bits 0-10: voxel of the brick)
+constexpr unsigned short kQueueCertain = 1u << 14;    // certainly accepted
+constexpr unsigned short kQueueBundleOnly = 1u << 15; // cannot win; bundle minimum only
+constexpr int kQueueCap = 64;
+
+struct WarpQueue {
+   unsigned slot[kQueueCap];       // position in the brick's segment list
+   unsigned short entry[kQueueCap];
+};
+
+// Exact evaluation of one queued candidate (reference arithmetic: two-float
+// fast path, FP64 replay) and its atomics.
+template <bool MULTI>
+__device__ __forceinline__ void brick_eval(const SegDev *__restrict__ segs,
+                                           const unsigned *__restrict__ list,
+                                           const LayerDev *__restrict__ layers, int layer_base,
+                                           unsigned slot, unsigned short e, int ox, int oy, int oz,
+                                           unsigned long long *skey, unsigned *sminb,
+                                           unsigned long long &n_slow) {
+   const unsigned s = list[slot];
+   const SegDev &S = segs[s];
+   const int li = e & (kBrickVoxels - 1);
+   const int x = ox + (li >> 8), y = oy + ((li >> 5) & 7), z = oz + (li & 31);
+   float dist_squ, r_sqr;
+   FastCand fc;
+   const float lpt[3] = {(float)(x - S.base[0]) + 0.5f, (float)(y - S.base[1]) + 0.5f,
+                         (float)(z - S.base[2]) + 0.5f};
+   if (S.pscale < 0x1p22f && fast_candidate(S, lpt, fc)) {
+      dist_squ = fc.dist_squ;
+      r_sqr = fc.r_sqr;
+   } else {
+      const double pt[3] = {(double)x + 0.5, (double)y + 0.5, (double)z + 0.5};
+      double cl[3];
+      exact_dist(S, pt, cl, dist_squ, r_sqr);
+      n_slow++;
+   }
+   if (dist_squ > layers[layer_base + S.bundle].f_ly_squ * r_sqr) // generator.cpp:329-331
+      return;
+   if (!(e & kQueueBundleOnly))
+      atomicMin(&skey[li], ((unsigned long long)__float_as_uint(dist_squ) << 32) |
+                               (unsigned long long)(0xFFFFFFFFu - s));
+   if (MULTI && !(e & kQueueCertain))
+      atomicMin(&sminb[li], (unsigned)S.bundle);
+}
+
+// EXACT pass, filter side: one segment over its sub-box; candidates that can
+// still win (or, for the bundle minimum, might be accepted) go to the warp's
+// queue, which is drained 32 entries at a time by all lanes together.
+template <bool MULTI>
+__device__ __forceinline__ void brick_filter(const SegDev &S, unsigned slot, const SubBox &b,
+                                             int ox, int oy, int oz, unsigned long long *skey,
+                                             WarpQueue &q, int &qn, int lane,
+                                             const SegDev *__restrict__ segs,
+                                             const unsigned *__restrict__ list,
+                                             const LayerDev *__restrict__ layers, int layer_base,
+                                             unsigned *sminb, unsigned long long &n_slow) {
+   const SegFP32 g = seg_fp32(S);
+   for (int k0 = 0; k0 < b.n; k0 += 32) {
+      const int k = k0 + lane;
+      bool need = false;
+      unsigned short e = 0;
+      if (k < b.n) {
+         int x, y, z;
+         sub_box_voxel(b, k, x, y, z);
+         float lo, hi;
+         candidate_bounds(g, x, y, z, lo, hi);
+         if (!(lo > g.thr)) { // inside the outermost layer at the thickest end
+            const bool certain = hi <= g.acc;
+            const int li = brick_index(x, y, z, ox, oy, oz);
+            // keys only decrease, so any value read bounds the final one from
+            // above; the initial ~0 reads as NaN and skips nothing
+            const unsigned long long cur =
+                *reinterpret_cast<volatile unsigned long long *>(&skey[li]);
+            const bool loser = lo > __uint_as_float((unsigned)(cur >> 32));
+            need = !(loser && (certain || !MULTI));
+            e = (unsigned short)(li | (certain ? kQueueCertain : 0) |
+                                 (loser ? kQueueBundleOnly : 0));
+         }
+      }
+      const unsigned m = __ballot_sync(0xFFFFFFFFu, need);
+      if (need) {
+         const int at = qn + __popc(m & ((1u << lane) - 1u));
+         q.slot[at] = slot;
+         q.entry[at] = e;
+      }
+      qn += __popc(m);
+      if (qn >= 32) { // drain 32 entries with every lane
+         __syncwarp();
+         const int at = qn - 32 + lane;
+         brick_eval<MULTI>(segs, list, layers, layer_base, q.slot[at], q.entry[at], ox, oy, oz,
+                           skey, sminb, n_slow);
+         qn -= 32;
+         __syncwarp();
+      }
+   }
+}
+
+// --------------------------------------------------------- winner decode ---
+// Label and orientation of voxel (x, y, z) of a tile from its winner key
+// (generator.cpp:343-372): the layer by lower_bound on the squared layer
+// scales, the vector by the layer's model ('p' segment direction, 'r'
+// radial, 'b' none).
+__device__ __forceinline__ void decode_voxel(unsigned long long key, int x, int y, int z,
+                                             const SegDev *__restrict__ segs,
+                                             const LayerDev *__restrict__ layers,
+                                             int layer_base, int max_layer, unsigned minb,
+                                             int32_t &label_out, float o[3],
+                                             unsigned long long &n_overlap,
+                                             unsigned long long &n_overflow,
+                                             unsigned long long &n_slow) {
+   o[0] = o[1] = o[2] = 0.f;
+   if (key == ~0ull) {
+      label_out = 0;
+      return;
+   }
+   const unsigned seg = 0xFFFFFFFFu - (unsigned)(key & 0xFFFFFFFFull);
+   const float dist_squ = __uint_as_float((unsigned)(key >> 32));
+   const SegDev &S = segs[seg];
+   const LayerDev &L = layers[layer_base + S.bundle];
+   // With a constant radius whose square rounds the same at every t
+   // (rsq_const) and at both ends, r^2 at the winner is known without
+   // evaluating the candidate again; only the radial model then needs it.
+   const bool r_known = S.rsq_const == S.rsq0 && S.rsq_const == S.rsq1; // false for NaN
+   FastCand fc;
+   bool fast = false, evaluated = false;
+   float r_sqr = S.rsq_const;
+   double cl[3];
+   auto evaluate = [&]() {
+      const float lpt[3] = {(float)(x - S.base[0]) + 0.5f, (float)(y - S.base[1]) + 0.5f,
+                            (float)(z - S.base[2]) + 0.5f};
+      fast = S.pscale < 0x1p22f && fast_candidate(S, lpt, fc);
+      float r2 = fc.r_sqr;
+      if (!fast) {
+         const double pt[3] = {(double)x + 0.5, (double)y + 0.5, (double)z + 0.5};
+         float d_chk;
+         exact_dist(S, pt, cl, d_chk, r2);
+      }
+      evaluated = true;
+      return r2;
+   };
+   if (!r_known)
+      r_sqr = evaluate();
+   // std::lower_bound(scale^2, double(dist_squ / r_sqr)) (generator.cpp:345-349)
+   const float qv = dist_squ / r_sqr;
+   int ly = 0;
+   while (ly < L.n && qv > L.sq_fdown[ly])
+      ly++;
+   label_out = ly + 1 + S.bundle * max_layer;
+   if (minb < (unsigned)S.bundle)
+      n_overlap++;
+   char m = 'b';
+   if (ly < L.n)
+      m = L.model[ly];
+   else
+      n_overflow++;
+   if (m == 'p') {
+      o[0] = S.vp[0];
+      o[1] = S.vp[1];
+      o[2] = S.vp[2];
+   } else if (m == 'r') {
+      if (!evaluated)
+         evaluate();
+      if (!(fast && fast_radial(S, fc, o))) {
+         const double pt[3] = {(double)x + 0.5, (double)y + 0.5, (double)z + 0.5};
+         if (fast) {
+            float d_chk, r_chk;
+            exact_dist(S, pt, cl, d_chk, r_chk);
+         }
+         n_slow++;
+         // vm::unit(point - closest) in the reference's double order
+         double nv[3] = {pt[0] - cl[0], pt[1] - cl[1], pt[2] - cl[2]};
+         double n2 = 0.0;
+         n2 = n2 + nv[0] * nv[0];
+         n2 = n2 + nv[1] * nv[1];
+         n2 = n2 + nv[2] * nv[2];
+         if (n2 > 0) {
+            const double inv = 1.0 / sqrt(n2);
+            nv[0] = nv[0] * inv;
+            nv[1] = nv[1] * inv;
+            nv[2] = nv[2] * inv;
+         }
+         o[0] = (float)nv[0];
+         o[1] = (float)nv[1];
+         o[2] = (float)nv[2];
+      }
+   }
+}
+
+// ------------------------------------------------------------- the brick ---
+template <bool MULTI>
+__global__ void __launch_bounds__(kBrickThreads, 3)
+voxel_bricks(const SegDev *__restrict__ segs, const TileDev *__restrict__ tiles, int64_t n_tiles,
+             int64_t n_bricks, const unsigned *__restrict__ offsets,
+             const unsigned *__restrict__ list, unsigned n_pairs,
+             const LayerDev *__restrict__ layers,
+             int32_t *const *__restrict__ labels, float *const *__restrict__ vecs,
+             unsigned long long *__restrict__ counters) {
+   __shared__ unsigned long long skey[kBrickVoxels];
+   __shared__ unsigned sminb[MULTI ? kBrickVoxels : 1];
+   __shared__ WarpQueue queues[kBrickWarps];
+   __shared__ unsigned s_next[2]; // next segment of the brick's list, per pass
+   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+   unsigned long long n_slow = 0, n_overlap = 0, n_overflow = 0;
+   for (int64_t brick = blockIdx.x; brick < n_bricks; brick += gridDim.x) {
+      // tile of the brick: last tile whose brick_base <= brick
+      int64_t lo = 0, hi = n_tiles - 1;
+      while (lo < hi) {
+         const int64_t mid = (lo + hi + 1) >> 1;
+         if (tiles[mid].brick_base <= brick)
+            lo = mid;
+         else
+            hi = mid - 1;
+      }
+      const TileDev &T = tiles[lo];
+      const int X = T.X, Y = T.Y, Z = T.Z;
+      const int64_t lb = brick - T.brick_base;
+      const int bz = (int)(lb % T.nb[2]);
+      const int64_t rxy = lb / T.nb[2];
+      const int by = (int)(rxy % T.nb[1]), bx = (int)(rxy / T.nb[1]);
+      const int ox = bx * kBrickX, oy = by * kBrickY, oz = bz * kBrickZ;
+      const int nx = min(kBrickX, X - ox), ny = min(kBrickY, Y - oy), nz = min(kBrickZ, Z - oz);
+      const int layer_base = T.layer_base, max_layer = T.max_layer;
+
+      for (int i = threadIdx.x; i < kBrickVoxels; i += kBrickThreads) {
+         skey[i] = ~0ull;
+         if (MULTI)
+            sminb[i] = ~0u;
+      }
+      if (threadIdx.x < 2)
+         s_next[threadIdx.x] = 0;
+      __syncthreads();
+      // (clamped to the planned list size: every slot below it is written)
+      const unsigned j1 = min(offsets[brick + 1], n_pairs), j0 = min(offsets[brick], j1);
+      // BOUND pass: warps take segments from a shared counter
+      for (;;) {
+         unsigned j = 0;
+         if (lane == 0)
+            j = atomicAdd(&s_next[0], 1u);
+         j = __shfl_sync(0xFFFFFFFFu, j, 0) + j0;
+         if (j >= j1)
+            break;
+         const SegDev &S = segs[list[j]];
+         SubBox b;
+         if (sub_box(S, ox, oy, oz, nx, ny, nz, b))
+            brick_bound<MULTI>(S, b, ox, oy, oz, skey, sminb, lane);
+      }
+      __syncthreads();
+      // EXACT pass
+      {
+         WarpQueue &q = queues[warp];
+         int qn = 0;
+         for (;;) {
+            unsigned j = 0;
+            if (lane == 0)
+               j = atomicAdd(&s_next[1], 1u);
+            j = __shfl_sync(0xFFFFFFFFu, j, 0) + j0;
+            if (j >= j1)
+               break;
+            const SegDev &S = segs[list[j]];
+            SubBox b;
+            if (sub_box(S, ox, oy, oz, nx, ny, nz, b))
+               brick_filter<MULTI>(S, j, b, ox, oy, oz, skey, q, qn, lane, segs, list, layers,
+                                   layer_base, sminb, n_slow);
+         }
+         __syncwarp();
+         if (lane < qn)
+            brick_eval<MULTI>(segs, list, layers, layer_base, q.slot[lane], q.entry[lane], ox, oy,
+                              oz, skey, sminb, n_slow);
+      }
+      __syncthreads();
+      // one warp per (x, y) row of the brick, lane = z: coalesced stores
+      int32_t *label = labels[lo];
+      float *vec = vecs[lo];
+      for (int r = warp; r < nx * ny; r += kBrickWarps) {
+         const int lx = r / ny, ly = r - (r / ny) * ny;
+         if (lane >= nz)
+            continue;
+         const int li = (lx * kBrickY + ly) * kBrickZ + lane;
+         const int x = ox + lx, y = oy + ly, z = oz + lane;
+         int32_t lab;
+         float o[3];
+         decode_voxel(skey[li], x, y, z, segs, layers, layer_base, max_layer,
+                      MULTI ? sminb[li] : ~0u, lab, o, n_overlap, n_overflow, n_slow);
+         const int64_t i = ((int64_t)x * Y + y) * Z + z;
+         label[i] = lab;
+         if (vec) {
+            vec[3 * i + 0] = o[0];
+            vec[3 * i + 1] = o[1];
+            vec[3 * i + 2] = o[2];
+         }
+      }
+      __syncthreads(); // shared keys are re-initialised for the next brick
+   }
+   if (n_overlap)
+      atomicAdd(&counters[0], n_overlap);
+   if (n_overflow)
+      atomicAdd(&counters[5], n_overflow);
+   if (n_slow)
+      atomicAdd(&counters[9], n_slow);
+}
+
+int launch_voxel_bricks(const SegDev *segs, const int32_t *seg_tile, int64_t n_segs,
+                        const TileDev *tiles, int64_t n_tiles, int64_t n_bricks, int64_t n_pairs,
+                        const LayerDev *layers, bool multi_bundle, int32_t *const *labels,
+                        float *const *vecs, void *ws, unsigned long long *counters,
+                        cudaStream_t st) {
+   if (n_tiles <= 0 || n_bricks <= 0)
+      return FPGB_OK;
+   if (n_pairs >= 0xFFFFFFFFll || n_segs >= 0xFFFFFFFFll) {
+      set_error("voxelizer: %lld segment-brick pairs exceed the 32-bit lists",
+                (long long)n_pairs);
+      return FPGB_EINVAL;
+   }
+   char *w = static_cast<char *>(ws);
+   auto *offsets = reinterpret_cast<unsigned *>(w);
+   w += align_up(sizeof(unsigned) * (n_bricks + 1), 256);
+   auto *counts = reinterpret_cast<unsigned *>(w);
+   w += align_up(sizeof(unsigned) * std::max<int64_t>(n_bricks, 1), 256);
+   auto *list = reinterpret_cast<unsigned *>(w);
+
+   FPGB_CUDA_TRY(cudaMemsetAsync(counts, 0, sizeof(unsigned) * n_bricks, st));
+   if (n_segs > 0) {
+      const unsigned g = (unsigned)std::min<int64_t>((n_segs + 255) / 256, 1 << 20);
+      brick_bin<false><<<g, 256, 0, st>>>(segs, seg_tile, n_segs, tiles, counts, nullptr,
+                                          nullptr, n_pairs, counters);
+      FPGB_CUDA_TRY(cudaGetLastError());
+   }
+   brick_scan<<<1, 1024, 0, st>>>(counts, n_bricks, offsets, counters);
+   FPGB_CUDA_TRY(cudaGetLastError());
+   if (n_segs > 0) {
+      FPGB_CUDA_TRY(cudaMemsetAsync(counts, 0, sizeof(unsigned) * n_bricks, st));
+      const unsigned g = (unsigned)std::min<int64_t>((n_segs + 255) / 256, 1 << 20);
+      brick_bin<true><<<g, 256, 0, st>>>(segs, seg_tile, n_segs, tiles, counts, offsets, list,
+                                         n_pairs, counters);
+      FPGB_CUDA_TRY(cudaGetLastError());
+   }
+   const unsigned grid = (unsigned)std::min<int64_t>(n_bricks, 0x7FFFFFFF);
+   if (multi_bundle)
+      voxel_bricks<true><<<grid, kBrickThreads, 0, st>>>(segs, tiles, n_tiles, n_bricks, offsets,
+                                                         list, (unsigned)n_pairs, layers, labels,
+                                                         vecs, counters);
+   else
+      voxel_bricks<false><<<grid, kBrickThreads, 0, st>>>(segs, tiles, n_tiles, n_bricks, offsets,
+                                                          list, (unsigned)n_pairs, layers, labels,
+                                                          vecs, counters);
+   FPGB_CUDA_TRY(cudaGetLastError());
+   return FPGB_OK;
+}
+
+} // namespace fpgb

@@ -118,12 +118,12 @@ int fpgb_generate_tissue_device(const fpgb_volume *vol,
  * reference (whose voxelizer runs on the host).  For callers that cannot call
  * cudaMalloc (device memory owned by another allocator, or code that must not
  * issue allocation calls): same inputs, outputs and results as
- * fpgb_generate_tissue_device, but the scratch (keys, per-voxel bundle
- * minima, segment/layer tables) lives in a fixed 64 MiB __device__ array of
- * this library that every GPU loading it holds until exit.  Problems needing
- * more scratch (about 8 bytes per voxel, 12 with several bundles, plus ~200
- * bytes per fiber segment) are rejected with FPGB_EINVAL before any device
- * work.  The first call on a device resolves the array's address with that
+ * fpgb_generate_tissue_device, but the scratch (segment and layer tables,
+ * segment lists of the 8x8x32-voxel bricks) lives in a fixed 64 MiB
+ * __device__ array of this library that every GPU loading it holds until
+ * exit.  Problems needing more scratch (about 280 bytes per fiber segment
+ * plus 4 per segment-brick overlap and 12 per brick: ~170,000 segments) are
+ * rejected with FPGB_EINVAL before any device work.  The first call on a device resolves the array's address with that
  * device current; make it before any stream capture.  All calls on a device
  * share the array: calls whose device work overlaps race and must be
  * serialised. */

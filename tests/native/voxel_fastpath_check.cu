@@ -13,6 +13,7 @@
 
 #include "../../fastpli_gb300/csrc/capi.cu"
 #include "../../fastpli_gb300/csrc/tissue.cu"
+#include "../../fastpli_gb300/csrc/voxel_bricks.cu"
 
 using namespace fpgb;
 
@@ -60,6 +61,7 @@ int main(int argc, char **argv) {
       return 2;
    }
    long long n = 0, fast = 0, bad = 0, vec_fast = 0, vec_bad = 0;
+   long long bound_bad = 0, certain = 0, certain_bad = 0;
    for (const SegDev &S : plan.segs) {
       for (int ix = 0; ix < S.ext[0]; ix++)
          for (int iy = 0; iy < S.ext[1]; iy++)
@@ -72,6 +74,22 @@ int main(int argc, char **argv) {
                const float lpt[3] = {(float)(x - S.base[0]) + 0.5f,
                                      (float)(y - S.base[1]) + 0.5f,
                                      (float)(z - S.base[2]) + 0.5f};
+               // FP32 estimate and its two-sided bound, and the certain-accept
+               // threshold of the two-pass key sweep
+               float mg;
+               const float d2f = approx_dist2(lpt[0] - S.pf[0], lpt[1] - S.pf[1],
+                                              lpt[2] - S.pf[2], S.vf[0], S.vf[1], S.vf[2],
+                                              S.c2f, S.c2_rcp, mg);
+               if (!((double)d_ex <= (double)d2f + mg && (double)d_ex >= (double)d2f - mg)) {
+                  if (bound_bad < 5)
+                     printf("BOUND dist %.9g estimate %.9g margin %.3g\n", d_ex, d2f, mg);
+                  bound_bad++;
+               }
+               if ((double)d2f + mg <= (double)S.acc_f) {
+                  certain++;
+                  if (d_ex > sc[2] * sc[2] * r_ex) // generator.cpp:329-331, outermost layer
+                     certain_bad++;
+               }
                FastCand fc;
                n++;
                if (!fast_candidate(S, lpt, fc))
@@ -98,7 +116,9 @@ int main(int argc, char **argv) {
                }
             }
    }
-   printf("candidates %lld fast %lld (%.6f) mismatches %lld vectors_fast %lld vector_mismatches %lld\n",
-          n, fast, n ? (double)fast / n : 0.0, bad, vec_fast, vec_bad);
-   return (bad || vec_bad) ? 1 : 0;
+   printf("candidates %lld fast %lld (%.6f) mismatches %lld vectors_fast %lld vector_mismatches %lld"
+          " bound_violations %lld certain %lld certain_rejected %lld\n",
+          n, fast, n ? (double)fast / n : 0.0, bad, vec_fast, vec_bad, bound_bad, certain,
+          certain_bad);
+   return (bad || vec_bad || bound_bad || certain_bad) ? 1 : 0;
 }

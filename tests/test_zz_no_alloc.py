@@ -17,7 +17,6 @@ import pytest
 import cases
 from fastpli_gb300 import _native as N
 
-pytestmark = pytest.mark.gpu
 
 
 def _inputs(c):
@@ -49,6 +48,7 @@ def _run(torch, fn, c, extra_ws=False):
     return label.cpu().numpy(), vector.cpu().numpy(), props, w.as_dict()
 
 
+@pytest.mark.gpu
 def test_noalloc_matches_device_entry_on_consecutive_calls(cuda):
     torch = cuda
     big = cases.synth_case(cases.crossing_small())   # two bundles, 307k voxels
@@ -64,13 +64,33 @@ def test_noalloc_matches_device_entry_on_consecutive_calls(cuda):
             assert got[3] == ref[3]
 
 
+def _oversize_case():
+    """300,000 short segments in a 64^3 volume: the segment table alone is
+    larger than the fixed scratch."""
+    rng = np.random.default_rng(5)
+    fibers = []
+    for _ in range(3000):
+        start = rng.uniform(4, 60, 3)
+        pts = start + np.cumsum(rng.normal(0, 0.3, (101, 3)), axis=0)
+        fibers.append(np.hstack([pts, np.full((101, 1), 0.5)]))
+    return dict(dim=np.array([64, 64, 64]), origin=np.zeros(3), voxel_size=1.0,
+                bundles=[fibers], layers=[[(1.0, 0.004, 1.0, "r")]])
+
+
+def test_oversize_case_needs_more_than_the_scratch():
+    c = _oversize_case()
+    flat, vol = _inputs(c)
+    assert N.load().fpgb_generate_workspace_size(N.byref(vol), N.byref(flat.struct)) > 64 << 20
+
+
+@pytest.mark.gpu
 def test_noalloc_rejects_problems_beyond_its_scratch(cuda):
     torch = cuda
-    c = dict(cases.gen_cases()["dimension"])
-    c["dim"] = np.array([512, 512, 64])  # 16.8 M voxels: 134 MB of keys
+    c = _oversize_case()
     flat, vol = _inputs(c)
     lib = N.load()
-    label = torch.empty(1, dtype=torch.int32, device="cuda")
+    # full-size output, so that nothing could land outside it in any case
+    label = torch.empty((64, 64, 64), dtype=torch.int32, device="cuda")
     rc = lib.fpgb_generate_tissue_noalloc(
         N.byref(vol), N.byref(flat.struct), 1, N.ptr(label), None, None, 0, None, None,
         torch.cuda.current_stream().cuda_stream)
