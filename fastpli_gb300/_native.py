@@ -85,6 +85,13 @@ _SIGS = {
     "fpgb_run_simulation_epa_device": ([_P, _P, _P, _P, _P, _I64, _D, _D, _P, _P,
                                         _P, _P, _P, _P], ctypes.c_int),
     "fpgb_count_steps": ([_P, _P, _D, _D], ctypes.c_int64),
+    "fpgb_optic_resample_size": ([_I64, _I64, _D, _P], ctypes.c_int),
+    "fpgb_optic_filter_resample_device": ([_P, _I64, _I64, _I64, _D, _D, _P, _P],
+                                          ctypes.c_int),
+    "fpgb_optic_filter_resample": ([_P, _I64, _I64, _I64, _D, _D, _P], ctypes.c_int),
+    "fpgb_optic_noise_device": ([_P, _I64, _D, ctypes.c_uint64, ctypes.c_uint64, _P, _P, _P],
+                                ctypes.c_int),
+    "fpgb_epa_device": ([_P, _I64, _I64, _P, _P, _P, _P], ctypes.c_int),
 }
 
 _lock = threading.Lock()

@@ -32,7 +32,8 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=o
           "-I", os.path.join(ROOT, "include")]
 PER_FILE = {"capi.cu": ["-Xcompiler", "-fopenmp"],
             "tissue.cu": ["-fmad=false", "-Xcompiler", "-fopenmp"],
-            "voxel_bricks.cu": ["-fmad=false"]}
+            "voxel_bricks.cu": ["-fmad=false"],
+            "optic.cu": ["-fmad=false"]}
 
 
 def _nvcc():

@@ -59,6 +59,7 @@ enum PoolSlot : int {
    kSlotProps,
    kSlotEpa,
    kSlotStaging,
+   kSlotOptic,
    kNumSlots
 };
 // Buffers are cached per (device, stream, slot): concurrent calls on

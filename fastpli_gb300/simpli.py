@@ -332,6 +332,71 @@ class Simpli:
             t[~mask], d[~mask], r[~mask] = 0, 0, 0
         return t, d, r
 
+    # ---------------------------------------------------------------- optic ---
+    def apply_optic_resample(self, data, shift=(0, 0), mp_pool=None):
+        """Gaussian blur + block-average resample of every polarizer angle
+        (__simpli.py:495-550).  ``data`` numpy [X, Y(, n_rho)] (host API) or a
+        float64 CUDA tensor (stays on the device).  ``mp_pool`` is accepted
+        and unused: all angles go to the GPU in one call."""
+        from . import optic
+        if self._optical_sigma is None:
+            raise ValueError("optical_sigma is None")
+        if self._voxel_size is None:
+            raise ValueError("voxel_size not set")
+        if self._pixel_size is None:
+            raise ValueError("pixel_size not set")
+        on_device = hasattr(data, "is_cuda") and data.is_cuda
+        if not on_device:
+            data = np.atleast_3d(np.array(data))
+        elif data.dim() == 2:
+            data = data[:, :, None]
+        if data.ndim > 3:
+            raise TypeError("data can be 1d, 2d or 3d")
+        shift = np.array(shift, int)
+        if shift.size != 2 or shift.ndim != 1:
+            raise TypeError("shift has to be (x,y)")
+        if shift[0] > 0 and shift[1] > 0:
+            data = data[shift[0]:, shift[1]:, ...]
+        scale = self._voxel_size / self._pixel_size
+        size = np.array(np.round(np.array(data.shape[0:2]) * scale), dtype=int)
+        if np.amin(size) == 0:
+            raise ValueError(f"voxel_size {self._voxel_size}, pixel_size {self._pixel_size} "
+                             f"and data shape {tuple(data.shape[0:2])} result in optical "
+                             f"image size of {size}")
+        if on_device:
+            out = optic.filter_resample_device(data.contiguous().double(),
+                                               self._optical_sigma, scale)
+            return out.squeeze()
+        return np.squeeze(optic.filter_resample(data, self._optical_sigma, scale))
+
+    def apply_optic(self, data, mp_pool=None):
+        """Resample, then the noise model (__simpli.py:462-489): returns
+        (resampled, noisy).  With a NegativeBinomialNoise model and device
+        data the noise is drawn on the device as well."""
+        from . import optic
+        if self._noise_model is None:
+            raise ValueError("noise_model not set")
+        resampled = self.apply_optic_resample(data, mp_pool=mp_pool)
+        on_device = hasattr(resampled, "is_cuda") and resampled.is_cuda
+        lo = float(resampled.min()) if on_device else np.amin(resampled)
+        if lo < 0:
+            raise AssertionError("intensity < 0 detected")
+        if on_device:
+            if isinstance(self._noise_model, optic.NegativeBinomialNoise):
+                return resampled, self._noise_model.device(resampled)
+            import torch
+            noisy = optic.add_noise(resampled.cpu().numpy(), self._noise_model)
+            return resampled, torch.from_numpy(np.asarray(noisy, np.float64)).to(resampled.device)
+        return resampled, optic.add_noise(resampled, self._noise_model)
+
+    def apply_epa_device(self, data, mask=None):
+        """epa of a device image stack in FP64 (epa.py:9-45) -> (t, d, r)."""
+        from . import optic
+        t, d, r = optic.epa_device(data)
+        if mask is not None:
+            t[~mask], d[~mask], r[~mask] = 0, 0, 0
+        return t, d, r
+
     # ------------------------------------------------- device-resident path ---
     def generate_tissue_device(self, only_tissue=False, stream=None):
         """Voxelize into HBM: (label, vector) torch CUDA tensors + props."""

@@ -174,6 +174,46 @@ int fpgb_run_simulation_epa_device(const fpgb_setup *setup, const int64_t *dim,
 int64_t fpgb_count_steps(const fpgb_setup *setup, const int64_t *dim,
                          double theta, double phi);
 
+/* ----------------------------------------------------------------------------
+ * Optic stage after the march.  Replaces fastpli.simulation.optic
+ * (src/fastpli/simulation/optic.py) as used by Simpli.apply_optic_resample /
+ * apply_optic (src/fastpli/simulation/__simpli.py:462-552).
+ * ------------------------------------------------------------------------- */
+
+/* Output size of resample (optic.py:100-101): int(round(X * scale)),
+ * int(round(Y * scale)), halves rounded to even. */
+int fpgb_optic_resample_size(int64_t X, int64_t Y, double scale, int64_t *out_dim);
+
+/* optic.filter_resample (optic.py:169-187) for every polarizer angle of an
+ * image stack [X, Y, n_rho] (the march's layout), into [SX, SY, n_rho]:
+ * Gaussian blur of width sigma / scale with scipy.ndimage.gaussian_filter
+ * semantics (axis 0 then 1, mode 'reflect', truncate 4.0, FP64; sigma == 0
+ * skips it), then the block-average resample of optic.py:85-120.  Device
+ * buffers; stream-ordered, no synchronisation. */
+int fpgb_optic_filter_resample_device(const double *d_image, int64_t X, int64_t Y,
+                                      int64_t n_rho, double sigma, double scale,
+                                      double *d_out, void *stream);
+/* Same with host buffers (synchronous). */
+int fpgb_optic_filter_resample(const double *image, int64_t X, int64_t Y, int64_t n_rho,
+                               double sigma, double scale, double *out);
+
+/* The negative-binomial CCD noise of the reference's pipelines
+ * (noise_model = lambda x: np.random.negative_binomial(x / (gain - 1),
+ * 1 / gain), tests/simulation/simpli_test.py:276-277): per pixel a Poisson
+ * draw of a Gamma(x / (gain - 1), scale gain - 1) rate, mean x, variance
+ * gain * x.  Pixel e's draw depends only on (seed, offset + e).  Pixels with
+ * x <= 0 or non-finite x are copied and counted in *n_invalid (numpy refuses
+ * n <= 0); when n_invalid is non-null the call synchronises to fill it.
+ * Device buffers. */
+int fpgb_optic_noise_device(const double *d_in, int64_t n, double gain, uint64_t seed,
+                            uint64_t offset, double *d_out, int64_t *n_invalid, void *stream);
+
+/* epa (src/fastpli/analysis/epa.py:9-45) of an image stack [n_pix, n_rho]
+ * (n_rho <= 64) in FP64: transmittance, direction, retardation maps.
+ * Device buffers; stream-ordered. */
+int fpgb_epa_device(const double *d_image, int64_t n_pix, int64_t n_rho, double *d_t,
+                    double *d_d, double *d_r, void *stream);
+
 /* Release the library's cached device pool on the current device. */
 int fpgb_release_pool(void);
 
