@@ -92,6 +92,8 @@ _SIGS = {
     "fpgb_optic_noise_device": ([_P, _I64, _D, ctypes.c_uint64, ctypes.c_uint64, _P, _P, _P],
                                 ctypes.c_int),
     "fpgb_epa_device": ([_P, _I64, _I64, _P, _P, _P, _P], ctypes.c_int),
+    "fpgb_rofl_device": ([_P, _I64, _I64, _D, _D, _D, ctypes.c_int, _P, _P, _P, _P],
+                         ctypes.c_int),
 }
 
 _lock = threading.Lock()

@@ -1,45 +1,92 @@
-"""epa modalities (transmittance, direction, retardation).
+"""Analysis of simulated image series on the GPU.
 
-Same arithmetic as fastpli.analysis.epa.epa (src/fastpli/analysis/epa.py:9-45):
-first Fourier harmonic over polarizer angles assumed equidistant in [0, pi).
-Accepts numpy arrays (host) or torch tensors (computed where they live).  The
-device ray march also fuses this epilogue
-(``_Simulator.run_simulation_device(..., epa=True)``).
+* ``epa(data)`` — transmittance, direction, retardation of an image stack
+  [..., n_rho] (src/fastpli/analysis/epa.py:9-45): first Fourier harmonic over
+  polarizer angles equidistant in [0, pi), computed in FP64 by the library's
+  ``epa_stack`` kernel.  numpy in -> numpy out (dtype of the input, as the
+  reference returns), CUDA tensor in -> CUDA tensors out.  The ray march also
+  fuses this epilogue (``_Simulator.run_simulation_device(..., epa=True)``).
+* ``rofl(data, ...)`` — ROFL tilt analysis of one pixel's 5-tilt series
+  (src/fastpli/analysis/rofl.py:16-63), and ``rofl_device`` for whole maps
+  [5, X, Y, n_rho] (one warp per pixel in ``rofl.cu``).
+
+There is no CPU path: everything runs in the native library.
 """
 
 import numpy as np
 
+from . import _native as N
+
+
+def _torch():
+    import torch
+    return torch
+
 
 def epa(data):
+    from . import optic
     if hasattr(data, "is_cuda"):
-        return _epa_torch(data)
+        torch = _torch()
+        out_dtype = torch.float32 if data.element_size() <= 4 else torch.float64
+        t, d, r = optic.epa_device(data.to(torch.float64))
+        return t.to(out_dtype), d.to(out_dtype), r.to(out_dtype)
     data = np.asarray(data)
-    dtype = np.float32 if data.itemsize <= 4 else np.float64
-    data = data.astype(dtype)
-    n = data.shape[-1]
-    rho_2 = 2 * np.linspace(0, np.pi, n, False, dtype=dtype)
-    a0 = np.sum(data, -1) / n
-    a1 = 2 * np.sum(data * np.sin(rho_2), -1) / n
-    b1 = 2 * np.sum(data * np.cos(rho_2), -1) / n
-    t = 2 * a0
-    d = 0.5 * np.arctan2(-b1, a1) + np.pi
-    a0[a0 < np.finfo(dtype).eps * 100] = 1
-    r = np.sqrt(a1 * a1 + b1 * b1) / a0
-    d = d % np.pi
-    return t, d, r
+    out_dtype = np.float32 if data.itemsize <= 4 else np.float64
+    torch = _torch()
+    dev = torch.from_numpy(np.ascontiguousarray(data, np.float64)).cuda()
+    return tuple(x.cpu().numpy().astype(out_dtype, copy=False) for x in optic.epa_device(dev))
 
 
-def _epa_torch(data):
-    import torch
-    dtype = torch.float32 if data.element_size() <= 4 else torch.float64
-    data = data.to(dtype)
-    n = data.shape[-1]
-    rho_2 = 2 * torch.arange(n, dtype=dtype, device=data.device) * (np.pi / n)
-    a0 = data.sum(-1) / n
-    a1 = 2 * (data * torch.sin(rho_2)).sum(-1) / n
-    b1 = 2 * (data * torch.cos(rho_2)).sum(-1) / n
-    t = 2 * a0
-    d = torch.remainder(0.5 * torch.atan2(-b1, a1) + np.pi, np.pi)
-    a0 = torch.where(a0 < torch.finfo(dtype).eps * 100, torch.ones_like(a0), a0)
-    r = torch.sqrt(a1 * a1 + b1 * b1) / a0
-    return t, d, r
+def _stream(stream):
+    torch = _torch()
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return s.cuda_stream
+
+
+def rofl_device(data, tilt_angle=np.deg2rad(5.5), gain=3, dir_offset=0, grad_mode=False,
+                mask=None, stream=None):
+    """ROFL of every pixel of a float64 CUDA tensor [5, X, Y, n_rho] (tilts
+    (0,0), (tau,0), (tau,90), (tau,180), (tau,270) degrees).  Returns a
+    [X, Y, 8] tensor: direction, inclination, t_rel, their standard
+    deviations, chi^2, model evaluations; NaN where ``mask`` (bool [X, Y])
+    is False."""
+    torch = _torch()
+    if not hasattr(data, "is_cuda") or not data.is_cuda:
+        raise TypeError("data must be a CUDA tensor")
+    if data.dim() != 4:
+        raise TypeError("data: [tilts, x, y, stack]")
+    if data.shape[0] != 5:
+        raise ValueError("data need 1 + 4 measurements")
+    if data.shape[-1] <= 3:
+        raise ValueError("data needs at least 3 equidistant rotations")
+    if gain <= 1:
+        raise ValueError("rofl gain <= 1")
+    d = data.to(torch.float64).contiguous()
+    X, Y, R = int(d.shape[1]), int(d.shape[2]), int(d.shape[3])
+    out = torch.empty((X, Y, 8), dtype=torch.float64, device=d.device)
+    m = None
+    if mask is not None:
+        m = torch.as_tensor(np.asarray(mask, bool) if not hasattr(mask, "is_cuda") else mask,
+                            device=d.device).to(torch.uint8).contiguous()
+        if tuple(m.shape) != (X, Y):
+            raise ValueError("mask must have shape (X, Y)")
+    bad = np.zeros(1, np.int64)
+    N.check(N.load().fpgb_rofl_device(N.ptr(d), X * Y, R, float(tilt_angle), float(gain),
+                                      float(dir_offset), int(bool(grad_mode)), N.ptr(m),
+                                      N.ptr(out), N.ptr(bad), _stream(stream)))
+    if bad[0]:
+        import warnings
+        warnings.warn(f"rofl: {int(bad[0])} pixels stopped at the evaluation limit")
+    return out
+
+
+def rofl(data, tilt_angle=np.deg2rad(5.5), gain=3, dir_offset=0, grad_mode=False):
+    """rofl.rofl for one pixel: data [5, n_rho] -> (direction, inclination,
+    t_rel, dir_dev, incl_dev, trel_dev, chi^2, evaluations)."""
+    data = np.asarray(data)
+    if data.ndim != 2:
+        raise TypeError("data: np.array([tilts,stack])")
+    torch = _torch()
+    dev = torch.from_numpy(np.ascontiguousarray(data, np.float64)).cuda()[:, None, None, :]
+    out = rofl_device(dev, tilt_angle, gain, dir_offset, grad_mode)
+    return tuple(float(v) for v in out[0, 0].cpu().numpy())

@@ -325,12 +325,54 @@ class Simpli:
         return images
 
     def apply_epa(self, data, mask=None):
-        """__simpli.py:597-621: transmittance, direction, retardation."""
+        """__simpli.py:597-621: transmittance, direction, retardation (NaN
+        outside ``mask``)."""
         from . import analysis
         t, d, r = analysis.epa(data)
         if mask is not None:
-            t[~mask], d[~mask], r[~mask] = 0, 0, 0
+            inv = ~np.asarray(mask, bool) if not hasattr(mask, "is_cuda") else ~mask
+            t[inv], d[inv], r[inv] = float("nan"), float("nan"), float("nan")
         return t, d, r
+
+    def apply_rofl(self, data, mask=None, mp_pool=None, grad_mode=False):
+        """ROFL of every pixel (__simpli.py:623-705): data [5, X, Y, n_rho]
+        for the tilts (0,0), (tau,0), (tau,90), (tau,180), (tau,270) degrees.
+        Returns directionmap, inclmap, trelmap, (dirdevmap, incldevmap,
+        treldevmap, funcmap, itermap); pixels outside ``mask`` are NaN (the
+        reference leaves them uninitialised).  numpy data -> numpy maps, CUDA
+        tensor -> CUDA maps.  ``mp_pool`` is accepted and unused."""
+        from . import analysis
+        if self._tilts is None:
+            raise ValueError("tilts not set")
+        tl = self._tilts
+        if tl.shape[0] != 5 or np.any(tl[:, 1] != np.deg2rad([0, 0, 90, 180, 270])) or \
+                tl[0, 0] != 0 or np.any(tl[1:, 0] != tl[1, 0]):
+            raise ValueError("tilts not suitable for ROFL")
+        tilt_angle = tl[1, 0]
+        on_device = hasattr(data, "is_cuda") and data.is_cuda
+        if on_device:
+            torch = analysis._torch()
+            out_dtype = torch.float32 if data.element_size() <= 4 else torch.float64
+            d = data
+        else:
+            data = np.asarray(data)
+            out_dtype = np.float32 if data.itemsize <= 4 else np.float64
+            import torch
+            d = torch.from_numpy(np.ascontiguousarray(data, np.float64)).cuda() \
+                if data.ndim == 4 else data
+        if d.ndim != 4:
+            raise TypeError("data: np.array([tilts,x,y,stack])")
+        if d.shape[0] != 5:
+            raise ValueError("data need 1 + 4 measurements")
+        if d.shape[-1] <= 3:
+            raise ValueError("data needs at least 3 equidistant rotations")
+        out = analysis.rofl_device(d, tilt_angle, 3, 0, grad_mode, mask)
+        maps = [out[:, :, i] for i in range(8)]
+        if on_device:
+            maps = [m.to(out_dtype) for m in maps]
+        else:
+            maps = [m.cpu().numpy().astype(out_dtype) for m in maps]
+        return maps[0], maps[1], maps[2], tuple(maps[3:])
 
     # ---------------------------------------------------------------- optic ---
     def apply_optic_resample(self, data, shift=(0, 0), mp_pool=None):

@@ -214,6 +214,24 @@ int fpgb_optic_noise_device(const double *d_in, int64_t n, double gain, uint64_t
 int fpgb_epa_device(const double *d_image, int64_t n_pix, int64_t n_rho, double *d_t,
                     double *d_d, double *d_r, void *stream);
 
+/* ROFL tilt analysis (src/fastpli/analysis/rofl.py:16-63 with
+ * _ROFL_with_jacobi.py, as Simpli.apply_rofl applies it per pixel,
+ * __simpli.py:623-705) of a 5-tilt series d_data [5, n_pix, n_rot] (tilts
+ * (0,0), (tau,0), (tau,90), (tau,180), (tau,270) degrees; 4 <= n_rot <= 32),
+ * FP64, one warp per pixel.  d_out [n_pix, 8] receives direction,
+ * inclination, t_rel, their standard deviations, chi^2 and the number of
+ * model evaluations of this implementation's Levenberg-Marquardt fit (the
+ * reference counts MINPACK's).  The fit uses the exact Jacobian of the
+ * reference's objective (the reference differentiates it by forward
+ * differences); grad_mode selects the reference's approximate Jacobian.  Pixels with
+ * d_mask[p] == 0 (d_mask may be null) get NaN.  When n_unconverged is
+ * non-null the call synchronises and stores the number of pixels that hit
+ * the evaluation limit. */
+int fpgb_rofl_device(const double *d_data, int64_t n_pix, int64_t n_rot, double tilt_angle,
+                     double gain, double dir_offset, int grad_mode,
+                     const unsigned char *d_mask, double *d_out, int64_t *n_unconverged,
+                     void *stream);
+
 /* Release the library's cached device pool on the current device. */
 int fpgb_release_pool(void);
 
