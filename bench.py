@@ -270,9 +270,13 @@ def run_gpu(args):
     value = ws * steps_per / (ms_step * 1e-3)
 
     # ----- e2e through the drop-in host API (numpy in/out) ---------------
-    e2e_steps = max(1, min(args.steps, 3))
-    lab_h, vec_h, props_h = g.run_generation()
-    sim.run_simulation(w.dim, lab_h, vec_h, props_h, 0.0, 0.0)
+    # two full untimed steps first: the first host-API step after the device
+    # loop pays one-off costs (pool growth, first touch of the host heap)
+    e2e_steps = max(1, min(args.steps, 5))
+    for _ in range(2):
+        lab_h, vec_h, props_h = g.run_generation()
+        for t, p in w.tilts:
+            sim.run_simulation(w.dim, lab_h, vec_h, props_h, float(t), float(p))
     torch.cuda.synchronize()
     if dist:
         dist.barrier()

@@ -1,9 +1,13 @@
 """Launch-configuration tuner for the batched march.
 
-The persistent march kernel has two knobs that change speed but never
-results: resident CTAs per SM and work items (128-ray blocks) taken per queue
-grab.  ``tune(batch)`` times a small grid of both on the batch itself (CUDA
-events, after a warm-up run) and keeps the fastest; choices are cached in a
+The persistent march kernel has three knobs that change speed but never
+results: resident CTAs per SM, work items (128-ray blocks) taken per queue
+grab, and the march variant for Lerp/Slerp (warp-cooperative with the
+interpolating steps compacted across the warp, or one thread per ray; both
+give the same bits).  ``tune(batch)`` times a small grid of all three on the
+batch itself (CUDA events, after a warm-up run) and keeps the fastest; the
+best variant depends on the tissue (sparse tiles favour the cooperative march,
+dense ones the per-thread march).  Choices are cached in a
 JSON file keyed by device, interpolation mode and a coarse shape bucket
 (pairs, mean steps per ray), so a later batch of the same kind skips the
 search.  Cache path: ``$FPGB_AUTOTUNE_CACHE`` or ``fastpli_gb300/_lib/autotune.json``.
@@ -17,7 +21,8 @@ import threading
 _LOCK = threading.Lock()
 _DEFAULT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "autotune.json")
 CTAS = (0, 4, 2)        # 0 = as many as fit
-GRABS = (1, 2, 4, 8)
+GRABS = (1, 2, 4)
+COOP = (1, 0)
 
 
 def cache_path():
@@ -48,35 +53,37 @@ def key(batch):
     pairs = int(batch.info.n_pairs)
     steps_per_ray = batch.steps / max(1, sum(
         int(t.dim[0]) * int(t.dim[1]) * len(batch.pairs_of(i)) for i, t in enumerate(batch.tiles)))
-    return f"{name}|interp{interp}|pairs2^{int(math.log2(max(1, pairs)))}|z2^{int(math.log2(max(1, steps_per_ray)))}"
+    return (f"{name}|interp{interp}|pairs2^{int(math.log2(max(1, pairs)))}"
+            f"|z2^{int(math.log2(max(1, steps_per_ray)))}|v3")
 
 
-def time_config(batch, ctas, grab, reps=3):
+def time_config(batch, ctas, grab, coop=1, reps=3):
     import torch
-    batch.run(ctas, grab)  # warm
+    batch.run(ctas, grab, coop)  # warm
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     for _ in range(reps):
-        batch.run(ctas, grab)
+        batch.run(ctas, grab, coop)
     e1.record()
     torch.cuda.synchronize()
     return e0.elapsed_time(e1) / reps
 
 
 def tune(batch, force=False, reps=3):
-    """Pick (ctas_per_sm, items_per_grab) for ``batch`` (already allocated);
+    """Pick (ctas_per_sm, items_per_grab, coop) for ``batch`` (already allocated);
     sets ``batch.config`` and returns (config, ms, table)."""
     k = key(batch)
     with _LOCK:
         cache = _load()
-    if not force and k in cache:
+    if not force and k in cache and len(cache[k]["config"]) == 3:
         batch.config = tuple(cache[k]["config"])
         return batch.config, cache[k]["ms"], None
     table = {}
     for c in CTAS:
         for g in GRABS:
-            table[(c, g)] = time_config(batch, c, g, reps)
+            for m in COOP:
+                table[(c, g, m)] = time_config(batch, c, g, m, reps)
     best = min(table, key=table.get)
     batch.config = best
     with _LOCK:

@@ -34,7 +34,7 @@ _SIGS = {
     "fpgb_batch_layout": ([_P, _P, _P, _P, _P, _P], ctypes.c_int),
     "fpgb_batch_props": ([_P, ctypes.c_int64, _P, ctypes.c_int64], ctypes.c_int),
     "fpgb_batch_upload": ([_P, _P, _P, _P], ctypes.c_int),
-    "fpgb_batch_run": ([_P, ctypes.c_int, ctypes.c_int, _P], ctypes.c_int),
+    "fpgb_batch_run": ([_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P], ctypes.c_int),
     "fpgb_batch_warnings": ([_P, _P, _P, _P], ctypes.c_int),
     "fpgb_batch_destroy": ([_P], ctypes.c_int),
 }
@@ -105,7 +105,7 @@ class TileBatch:
         self.arena = None
         self.workspace = None
         self._graph = None
-        self.config = (0, 0)
+        self.config = (0, 0, 1)
 
     # ------------------------------------------------------------ sizes ---
     @property
@@ -134,11 +134,12 @@ class TileBatch:
                                         self.workspace.data_ptr(), _stream(stream)))
         return self
 
-    def run(self, ctas_per_sm=None, items_per_grab=None, stream=None):
-        c, g = self.config
+    def run(self, ctas_per_sm=None, items_per_grab=None, coop=None, stream=None):
+        c, g, k = (tuple(self.config) + (1,))[:3]
         c = c if ctas_per_sm is None else ctas_per_sm
         g = g if items_per_grab is None else items_per_grab
-        N.check(lib().fpgb_batch_run(self._h, int(c), int(g), _stream(stream)))
+        k = k if coop is None else coop
+        N.check(lib().fpgb_batch_run(self._h, int(c), int(g), int(k), _stream(stream)))
 
     def capture(self):
         """Capture the batch's launch sequence into a CUDA graph."""

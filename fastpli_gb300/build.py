@@ -11,6 +11,11 @@ Flags that matter for parity:
   * ``tissue.cu``, ``voxel_bricks.cu``: ``-fmad=false`` — the voxelizer's
     exact double path must round every product and sum separately, as the
     reference does.
+  * ``raymarch.cu``, ``batch.cu``: ``-fmad=false`` with the wanted fused
+    multiply-adds written out — every march kernel (plain or batched,
+    per-thread or cooperative) then gives the same bits for the same tile.
+  * ``optic.cu``: ``-fmad=false`` — the Gaussian filter sums in scipy's
+    order with separate roundings.
 """
 
 import concurrent.futures as cf
@@ -33,7 +38,9 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=o
 PER_FILE = {"capi.cu": ["-Xcompiler", "-fopenmp"],
             "tissue.cu": ["-fmad=false", "-Xcompiler", "-fopenmp"],
             "voxel_bricks.cu": ["-fmad=false"],
-            "optic.cu": ["-fmad=false"]}
+            "optic.cu": ["-fmad=false"],
+            "raymarch.cu": ["-fmad=false"],
+            "batch.cu": ["-fmad=false"]}
 
 
 def _nvcc():

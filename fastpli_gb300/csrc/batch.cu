@@ -65,7 +65,7 @@ struct fpgb_batch_impl {
    int rays_per_item = 0;
    int64_t n_untilted = 0; // items [0, n_untilted) untilted, the rest tilted
    int sms = 1;
-   int fit[2] = {1, 1}; // resident CTAs per SM of the untilted / tilted march
+   int fit[2][2] = {{1, 1}, {1, 1}}; // resident CTAs per SM: [untilted / tilted][per-thread / coop]
 };
 
 // ----------------------------------------------------------------------------
@@ -77,7 +77,7 @@ struct fpgb_batch_impl {
 static_assert(sizeof(MarchParams) % 16 == 0, "MarchParams is copied as int4");
 constexpr int kBatchThreads = 128; // one work item = one CTA-width block of rays
 
-template <int MODE, bool TILT>
+template <int MODE, bool TILT, bool COOP>
 __global__ void __launch_bounds__(128)
 batch_march(const MarchParams *__restrict__ prm, const BatchItem *__restrict__ items,
             int64_t n_items, int chunk, unsigned long long *__restrict__ next,
@@ -86,7 +86,7 @@ batch_march(const MarchParams *__restrict__ prm, const BatchItem *__restrict__ i
    // the item's parameter block, staged in shared memory (read like the
    // plain kernel reads its by-value parameters)
    __shared__ __align__(16) MarchParams sP;
-   __shared__ CoopScratch scratch[kBatchThreads / 32];
+   __shared__ CoopScratch scratch[COOP ? kBatchThreads / 32 : 1];
    int cur = -1;
    for (;;) {
       if (threadIdx.x == 0)
@@ -112,7 +112,7 @@ batch_march(const MarchParams *__restrict__ prm, const BatchItem *__restrict__ i
             if ((int)threadIdx.x < w.ray_count)
                march_one_ray_column(sP, w.ray_begin + threadIdx.x, sP.label, sP.vec, sP.image,
                                     sP.epa_t, sP.epa_d, sP.epa_r, counters);
-         } else if (MODE == 0) {
+         } else if (MODE == 0 || !COOP) {
             if ((int)threadIdx.x < w.ray_count)
                march_one_ray<MODE, TILT>(sP, w.ray_begin + threadIdx.x, sP.label, sP.vec,
                                          sP.image, sP.epa_t, sP.epa_d, sP.epa_r, counters);
@@ -128,22 +128,30 @@ batch_march(const MarchParams *__restrict__ prm, const BatchItem *__restrict__ i
 }
 
 template <int MODE, bool TILT>
-int batch_march_fit(int *fit) {
-   FPGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(fit, batch_march<MODE, TILT>,
-                                                              kBatchThreads, 0));
+int batch_march_fit(int fit[2]) {
+   FPGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+       &fit[0], batch_march<MODE, TILT, false>, kBatchThreads, 0));
+   FPGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+       &fit[1], batch_march<MODE, TILT, true>, kBatchThreads, 0));
    return FPGB_OK;
 }
 
 template <int MODE, bool TILT>
 int launch_batch_march(const MarchParams *prm, const BatchItem *items, int64_t n_items,
-                       unsigned long long *next, unsigned long long *counters, int sms, int fit,
-                       int ctas_per_sm, int chunk, cudaStream_t st) {
+                       unsigned long long *next, unsigned long long *counters, int sms,
+                       const int fits[2], int ctas_per_sm, int chunk, int coop, cudaStream_t st) {
    if (n_items <= 0)
       return FPGB_OK;
+   const bool cp = MODE != 0 && coop != 0;
+   const int fit = fits[cp ? 1 : 0];
    const int per_sm = std::max(1, std::min(ctas_per_sm > 0 ? ctas_per_sm : fit, fit));
    const int64_t grid = std::min<int64_t>((int64_t)sms * per_sm, (n_items + chunk - 1) / chunk);
-   batch_march<MODE, TILT><<<(unsigned)grid, kBatchThreads, 0, st>>>(prm, items, n_items, chunk,
-                                                                     next, counters);
+   if (cp)
+      batch_march<MODE, TILT, true><<<(unsigned)grid, kBatchThreads, 0, st>>>(
+          prm, items, n_items, chunk, next, counters);
+   else
+      batch_march<MODE, TILT, false><<<(unsigned)grid, kBatchThreads, 0, st>>>(
+          prm, items, n_items, chunk, next, counters);
    FPGB_CUDA_TRY(cudaGetLastError());
    return FPGB_OK;
 }
@@ -369,16 +377,16 @@ int upload_batch(fpgb_batch_impl *B, void *arena, void *ws, cudaStream_t st) {
    B->sms = sm_count_now();
    switch (B->setup.interpolate) {
    case 0:
-      FPGB_TRY((batch_march_fit<0, false>(&B->fit[0])));
-      FPGB_TRY((batch_march_fit<0, true>(&B->fit[1])));
+      FPGB_TRY((batch_march_fit<0, false>(B->fit[0])));
+      FPGB_TRY((batch_march_fit<0, true>(B->fit[1])));
       break;
    case 1:
-      FPGB_TRY((batch_march_fit<1, false>(&B->fit[0])));
-      FPGB_TRY((batch_march_fit<1, true>(&B->fit[1])));
+      FPGB_TRY((batch_march_fit<1, false>(B->fit[0])));
+      FPGB_TRY((batch_march_fit<1, true>(B->fit[1])));
       break;
    default:
-      FPGB_TRY((batch_march_fit<2, false>(&B->fit[0])));
-      FPGB_TRY((batch_march_fit<2, true>(&B->fit[1])));
+      FPGB_TRY((batch_march_fit<2, false>(B->fit[0])));
+      FPGB_TRY((batch_march_fit<2, true>(B->fit[1])));
       break;
    }
    return FPGB_OK;
@@ -387,7 +395,7 @@ int upload_batch(fpgb_batch_impl *B, void *arena, void *ws, cudaStream_t st) {
 
 // All device work of one batch: no allocation, no host synchronisation, so
 // a stream capture of this call is a complete graph of the batch.
-int run_batch(fpgb_batch_impl *B, int march_ctas_per_sm, int chunk, cudaStream_t st) {
+int run_batch(fpgb_batch_impl *B, int march_ctas_per_sm, int chunk, int coop, cudaStream_t st) {
    if (!B->arena || !B->ws) {
       set_error("batch: buffers not bound (call fpgb_batch_upload first)");
       return FPGB_EINVAL;
@@ -415,9 +423,9 @@ int run_batch(fpgb_batch_impl *B, int march_ctas_per_sm, int chunk, cudaStream_t
    const int ch = chunk > 0 ? chunk : 4;
 #define FPGB_BATCH_MARCH(M)                                                                    \
    FPGB_TRY((launch_batch_march<M, false>(prm, items, n0, next, counters, B->sms, B->fit[0],   \
-                                          march_ctas_per_sm, ch, st)));                        \
+                                          march_ctas_per_sm, ch, coop, st)));                        \
    FPGB_TRY((launch_batch_march<M, true>(prm, items + n0, n1, next + 1, counters, B->sms,      \
-                                         B->fit[1], march_ctas_per_sm, ch, st)))
+                                         B->fit[1], march_ctas_per_sm, ch, coop, st)))
    switch (B->setup.interpolate) {
    case 0: FPGB_BATCH_MARCH(0); break;
    case 1: FPGB_BATCH_MARCH(1); break;
@@ -513,12 +521,13 @@ int fpgb_batch_upload(fpgb_batch *b, void *d_arena, void *d_workspace, void *str
    return upload_batch(b, d_arena, d_workspace, as_stream(stream));
 }
 
-int fpgb_batch_run(fpgb_batch *b, int march_ctas_per_sm, int items_per_grab, void *stream) {
+int fpgb_batch_run(fpgb_batch *b, int march_ctas_per_sm, int items_per_grab, int march_coop,
+                   void *stream) {
    if (!b) {
       set_error("batch: null handle");
       return FPGB_EINVAL;
    }
-   return run_batch(b, march_ctas_per_sm, items_per_grab, as_stream(stream));
+   return run_batch(b, march_ctas_per_sm, items_per_grab, march_coop, as_stream(stream));
 }
 
 int fpgb_batch_warnings(const fpgb_batch *b, fpgb_warnings *w, int64_t *fp64_replays,

@@ -1,5 +1,13 @@
 // Device side of the ray march shared by the plain kernel (raymarch.cu)
 // and the persistent batched kernel (batch.cu).
+//
+// Both translation units are compiled with -fmad=false and the fused
+// multiply-adds of the hot arithmetic are written out (fmaf): the compiler
+// then contracts nothing on its own, and the same source gives the same bits
+// in every kernel that inlines it — plain or batched, per-thread or
+// cooperative march, column path — whatever the surrounding code.  (With
+// contraction left to the compiler, the same column code inlined into two
+// kernels differed in the last bit of a few pixels.)
 #pragma once
 
 #include <cuda_runtime.h>
@@ -15,7 +23,9 @@ struct F3 {
    float x, y, z;
 };
 __device__ __forceinline__ bool is_zero(F3 v) { return v.x == 0.f && v.y == 0.f && v.z == 0.f; }
-__device__ __forceinline__ float dot3(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float dot3(F3 a, F3 b) {
+   return fmaf(a.z, b.z, fmaf(a.y, b.y, a.x * b.x));
+}
 
 __device__ __forceinline__ F3 load_vec(const float *__restrict__ vec, int64_t idx) {
    const float *p = vec + 3 * idx;
@@ -78,7 +88,7 @@ __device__ __forceinline__ F3 slerp_axis(F3 v, F3 u, float t) {
       w0 = __sinf((1.f - t) * th) * inv;
       w1 = __sinf(t * th) * inv;
    }
-   return F3{v.x * w0 + u.x * w1, v.y * w0 + u.y * w1, v.z * w0 + u.z * w1};
+   return F3{fmaf(v.x, w0, u.x * w1), fmaf(v.y, w0, u.y * w1), fmaf(v.z, w0, u.z * w1)};
 }
 
 template <int MODE>
@@ -261,26 +271,6 @@ __device__ __forceinline__ void sincos_small(float x, float &s, float &c) {
    }
 }
 
-// One birefringent step on the unit state (u1, u2, u3).
-__device__ __forceinline__ void retard(float &u1, float &u2, float &u3, F3 v, float n2,
-                                       float kret) {
-   const float xx = v.x * v.x, yy = v.y * v.y;
-   const float q = xx + yy;
-   if (q > 0.f) {
-      const float ret = kret * q * rsqrtf(n2);
-      float sr, cr;
-      sincos_small(ret, sr, cr);
-      const float iq = __fdividef(1.f, q);
-      const float c = (xx - yy) * iq, s = 2.f * v.x * v.y * iq;
-      const float a1 = u1 * c - u2 * s;
-      const float c1 = u1 * s + u2 * c;
-      const float b1 = c1 * cr + u3 * sr;
-      u3 = -c1 * sr + u3 * cr;
-      u1 = a1 * c + b1 * s;
-      u2 = -a1 * s + b1 * c;
-   }
-}
-
 // Analyser and the rho / epa epilogue of one ray (simulator.cpp:346-362,
 // epa.py:31-43), plus its warning / status counters.
 __device__ __forceinline__ void ray_epilogue(const MarchParams &P, int64_t ray, float u1, float u2,
@@ -294,12 +284,12 @@ __device__ __forceinline__ void ray_epilogue(const MarchParams &P, int64_t ray, 
    float a0 = 0.f, a1 = 0.f, b1 = 0.f;
    double *out = image + ray * P.n_rho;
    for (int r = 0; r < P.n_rho; r++) {
-      const float I = amp * (1.f - u1 * P.c2r[r] + u2 * P.s2r[r]);
+      const float I = amp * fmaf(u2, P.s2r[r], fmaf(-u1, P.c2r[r], 1.f));
       if (image)
          out[r] = widen(I);
       a0 += I;
-      a1 += I * P.epa_sin[r];
-      b1 += I * P.epa_cos[r];
+      a1 = fmaf(I, P.epa_sin[r], a1);
+      b1 = fmaf(I, P.epa_cos[r], b1);
    }
    if (epa_t || epa_d || epa_r) {
       const float n = (float)P.n_rho;
@@ -344,7 +334,7 @@ __device__ __forceinline__ void ray_setup(const MarchParams &P, int64_t ray, int
 __device__ __forceinline__ bool retard_params(F3 v, float n2, float kret, float &c, float &s,
                                               float &cr, float &sr) {
    const float xx = v.x * v.x, yy = v.y * v.y;
-   const float q = xx + yy;
+   const float q = fmaf(v.x, v.x, yy);
    if (!(q > 0.f))
       return false;
    const float ret = kret * q * rsqrtf(n2);
@@ -359,12 +349,12 @@ __device__ __forceinline__ bool retard_params(F3 v, float n2, float kret, float 
 // rho-free frame).
 __device__ __forceinline__ void apply_retard(float &u1, float &u2, float &u3, float c, float s,
                                              float cr, float sr) {
-   const float a1 = u1 * c - u2 * s;
-   const float c1 = u1 * s + u2 * c;
-   const float b1 = c1 * cr + u3 * sr;
-   u3 = -c1 * sr + u3 * cr;
-   u1 = a1 * c + b1 * s;
-   u2 = -a1 * s + b1 * c;
+   const float a1 = fmaf(u1, c, -u2 * s);
+   const float c1 = fmaf(u1, s, u2 * c);
+   const float b1 = fmaf(c1, cr, u3 * sr);
+   u3 = fmaf(-c1, sr, u3 * cr);
+   u1 = fmaf(a1, c, b1 * s);
+   u2 = fmaf(-a1, s, b1 * c);
 }
 
 // One CCD-pixel ray, one thread, every step in order.  Used for NN, where a
@@ -425,9 +415,9 @@ __device__ __forceinline__ void march_one_ray(const MarchParams &P, int64_t ray,
       if (n2 - 1.f > 1e-5f)
          w_norm = true;
       if (TILT && P.rotate) {
-         v = F3{P.rot[0] * v.x + P.rot[1] * v.y + P.rot[2] * v.z,
-                P.rot[3] * v.x + P.rot[4] * v.y + P.rot[5] * v.z,
-                P.rot[6] * v.x + P.rot[7] * v.y + P.rot[8] * v.z};
+         v = F3{dot3(F3{P.rot[0], P.rot[1], P.rot[2]}, v),
+                dot3(F3{P.rot[3], P.rot[4], P.rot[5]}, v),
+                dot3(F3{P.rot[6], P.rot[7], P.rot[8]}, v)};
       }
       float c, s, cr, sr;
       if (retard_params(v, n2, o.kret, c, s, cr, sr))
@@ -441,7 +431,7 @@ __device__ __forceinline__ void march_one_ray(const MarchParams &P, int64_t ray,
 // Vertical ray through its whole column in order (MarchParams::column):
 // labels and axes stream in as 16-byte loads, four voxels at a time (the
 // column starts 16-byte aligned because Z % 4 == 0).  Same arithmetic per
-// step as march_one_ray.  Interpolation modes need nothing else here: at the
+// step as the warp march.  Interpolation modes need nothing else here: at the
 // exact voxel centres of such a ray every interpolation axis collapses.
 __device__ __forceinline__ void march_one_ray_column(const MarchParams &P, int64_t ray,
                                                      const int32_t *__restrict__ label,
@@ -599,9 +589,9 @@ __device__ __forceinline__ void coop_job(const MarchParams &P, const int32_t *__
       const float n2 = dot3(v, v);
       status = (n2 - 1.f > 1e-5f) ? kJobNorm : 0;
       if (TILT && P.rotate) {
-         v = F3{P.rot[0] * v.x + P.rot[1] * v.y + P.rot[2] * v.z,
-                P.rot[3] * v.x + P.rot[4] * v.y + P.rot[5] * v.z,
-                P.rot[6] * v.x + P.rot[7] * v.y + P.rot[8] * v.z};
+         v = F3{dot3(F3{P.rot[0], P.rot[1], P.rot[2]}, v),
+                dot3(F3{P.rot[3], P.rot[4], P.rot[5]}, v),
+                dot3(F3{P.rot[6], P.rot[7], P.rot[8]}, v)};
       }
       if (!retard_params(v, n2, P.lut[lab].kret, c, s, cr, sr))
          status |= kJobIdentity;

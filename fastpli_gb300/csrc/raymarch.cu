@@ -307,7 +307,7 @@ int plan_march(const fpgb_setup *s, const int64_t *dim, const double *props, int
 // ======================================================================
 // device
 // ======================================================================
-template <int MODE, bool TILT>
+template <int MODE, bool TILT, bool COOP>
 __global__ void __launch_bounds__(128)
 march_rays(const MarchParams P, const int32_t *__restrict__ label,
            const float *__restrict__ vec, double *__restrict__ image,
@@ -317,10 +317,9 @@ march_rays(const MarchParams P, const int32_t *__restrict__ label,
    if (!TILT && P.column) {
       if (ray < P.X * P.Y)
          march_one_ray_column(P, ray, label, vec, image, epa_t, epa_d, epa_r, counters);
-   } else if (MODE == 0) {
-      if (ray >= P.X * P.Y)
-         return;
-      march_one_ray<MODE, TILT>(P, ray, label, vec, image, epa_t, epa_d, epa_r, counters);
+   } else if (MODE == 0 || !COOP) {
+      if (ray < P.X * P.Y)
+         march_one_ray<MODE, TILT>(P, ray, label, vec, image, epa_t, epa_d, epa_r, counters);
    } else { // whole warps take part in the cooperative march
       __shared__ CoopScratch scratch[4];
       march_ray_coop<MODE, TILT>(P, ray, ray < P.X * P.Y, label, vec, image, epa_t, epa_d,
@@ -389,15 +388,24 @@ int launch_march(const MarchPlan &mp, const int32_t *d_label, const float *d_vec
    const int64_t n_rays = P.X * P.Y;
    const unsigned grid = (unsigned)((n_rays + 127) / 128);
    const bool tilt = P.rotate || P.dx_fx != 0 || P.dy_fx != 0;
-#define FPGB_LAUNCH(M, T)                                                                  \
-   march_rays<M, T><<<grid, 128, 0, st>>>(P, d_label, d_vec, d_image, d_t, d_d, d_r, d_counters)
-   switch (P.mode * 2 + (tilt ? 1 : 0)) {
-   case 0: FPGB_LAUNCH(0, false); break;
-   case 1: FPGB_LAUNCH(0, true); break;
-   case 2: FPGB_LAUNCH(1, false); break;
-   case 3: FPGB_LAUNCH(1, true); break;
-   case 4: FPGB_LAUNCH(2, false); break;
-   default: FPGB_LAUNCH(2, true); break;
+   // separate kernels per march variant: the cooperative one holds 36 KB of
+   // shared scratch and more registers, which must not cap the occupancy of
+   // the per-thread one
+#define FPGB_LAUNCH(M, T, C)                                                               \
+   march_rays<M, T, C><<<grid, 128, 0, st>>>(P, d_label, d_vec, d_image, d_t, d_d, d_r,      \
+                                             d_counters)
+   const bool coop = P.coop != 0;
+   switch (P.mode * 4 + (tilt ? 2 : 0) + (coop ? 1 : 0)) {
+   case 0: case 1: FPGB_LAUNCH(0, false, false); break;
+   case 2: case 3: FPGB_LAUNCH(0, true, false); break;
+   case 4: FPGB_LAUNCH(1, false, false); break;
+   case 5: FPGB_LAUNCH(1, false, true); break;
+   case 6: FPGB_LAUNCH(1, true, false); break;
+   case 7: FPGB_LAUNCH(1, true, true); break;
+   case 8: FPGB_LAUNCH(2, false, false); break;
+   case 9: FPGB_LAUNCH(2, false, true); break;
+   case 10: FPGB_LAUNCH(2, true, false); break;
+   default: FPGB_LAUNCH(2, true, true); break;
    }
 #undef FPGB_LAUNCH
    FPGB_CUDA_TRY(cudaGetLastError());

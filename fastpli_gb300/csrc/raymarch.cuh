@@ -54,7 +54,13 @@ struct MarchParams {
    int32_t tilted; // x/y advance or the axis rotates
    int32_t column; // vertical ray reading z = 0..Z-1 (or mirrored) in order,
                    // Z % 4 == 0: the vectorised column path applies
+   // Lerp/Slerp rays that are not vertical columns: 1 = warp-cooperative
+   // march (steps needing interpolation compacted across the warp), 0 = one
+   // thread per ray.  Both give the same bits; the choice is speed only.
+   int32_t coop;
+   int32_t pad_[3];
 };
+static_assert(sizeof(MarchParams) % 16 == 0, "MarchParams is staged in 16-byte words");
 
 struct MarchPlan {
    MarchParams prm;

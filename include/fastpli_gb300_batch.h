@@ -63,10 +63,12 @@ int fpgb_batch_upload(fpgb_batch *b, void *d_arena, void *d_workspace,
                       void *stream);
 /* Launch configuration: march_ctas_per_sm (<= 0: as many as fit) resident
  * CTAs per SM for the persistent march; items_per_grab (<= 0: 4) work items
- * of 128 rays taken per queue access.  Both are tuning knobs only (results do
- * not depend on them); fastpli_gb300.autotune picks them. */
+ * of 128 rays taken per queue access; march_coop (Lerp/Slerp) 1 = steps that
+ * need interpolation are compacted across each warp, 0 = one thread per ray.
+ * All three are tuning knobs only (results are bit-identical across them);
+ * fastpli_gb300.autotune picks them. */
 int fpgb_batch_run(fpgb_batch *b, int march_ctas_per_sm, int items_per_grab,
-                   void *stream);
+                   int march_coop, void *stream);
 /* Synchronises; fails with FPGB_EINVAL when a label was out of range.
  * fp64_replays (may be NULL) counts voxelizer candidates decided in FP64. */
 int fpgb_batch_warnings(const fpgb_batch *b, fpgb_warnings *w,

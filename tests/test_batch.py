@@ -54,11 +54,15 @@ def test_symbols_exported():
 
 
 @pytest.mark.gpu
-def test_batch_bit_identical_to_single_volume_path(cuda):
+@pytest.mark.parametrize("coop", [0, 1])
+def test_batch_bit_identical_to_single_volume_path(cuda, coop):
+    """Either march variant of the batch (per-thread or warp-cooperative)
+    gives the single-volume path's bits."""
     torch = cuda
     tiles = small_tiles()
     kw = tiles[0].setup_kwargs()
     b = B.TileBatch(tiles, kw, epa=True).allocate()
+    b.config = (0, 0, coop)
     b.run()
     torch.cuda.synchronize()
     w = b.warnings()
