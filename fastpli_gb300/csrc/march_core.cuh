@@ -428,6 +428,26 @@ __device__ __forceinline__ void march_one_ray(const MarchParams &P, int64_t ray,
                 counters);
 }
 
+// Rays of a 128-thread block: a 4 (x) x 32 (y) tile of CCD pixels.  The
+// per-thread march gives each warp a 4 x 8 patch of it: the 8-corner
+// neighbourhoods of the warp's rays then cover 5 x 9 voxel columns instead of
+// the 2 x 33 of 32 rays in a line, so more of each step's gathers hit the
+// same L1 lines (5% faster on config 2).  The cooperative march keeps a line
+// of 32 rays per warp (x fixed), which suits its compaction better.  Returns
+// false for tile positions outside the image.
+constexpr int kRayTileX = 4, kRayTileY = 32;
+
+template <bool COOP>
+__device__ __forceinline__ bool tile_ray(const MarchParams &P, int64_t tile, int tid,
+                                         int64_t &ray) {
+   const int64_t nby = (P.Y + kRayTileY - 1) / kRayTileY;
+   const int w = tid >> 5, l = tid & 31;
+   const int64_t x = (tile / nby) * kRayTileX + (COOP ? w : (l >> 3));
+   const int64_t y = (tile % nby) * kRayTileY + (COOP ? l : w * 8 + (l & 7));
+   ray = x * P.Y + y;
+   return x < P.X && y < P.Y;
+}
+
 // Vertical ray through its whole column in order (MarchParams::column):
 // labels and axes stream in as 16-byte loads, four voxels at a time (the
 // column starts 16-byte aligned because Z % 4 == 0).  Same arithmetic per

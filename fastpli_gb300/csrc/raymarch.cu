@@ -313,16 +313,20 @@ march_rays(const MarchParams P, const int32_t *__restrict__ label,
            const float *__restrict__ vec, double *__restrict__ image,
            double *__restrict__ epa_t, double *__restrict__ epa_d, double *__restrict__ epa_r,
            unsigned long long *__restrict__ counters) {
-   const int64_t ray = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-   if (!TILT && P.column) {
+   if (!TILT && P.column) { // 128 consecutive vertical rays per block
+      const int64_t ray = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
       if (ray < P.X * P.Y)
          march_one_ray_column(P, ray, label, vec, image, epa_t, epa_d, epa_r, counters);
-   } else if (MODE == 0 || !COOP) {
-      if (ray < P.X * P.Y)
+      return;
+   }
+   int64_t ray; // one 4 x 32 tile of rays per block (tile_ray)
+   const bool valid = tile_ray<MODE != 0 && COOP>(P, blockIdx.x, threadIdx.x, ray);
+   if (MODE == 0 || !COOP) {
+      if (valid)
          march_one_ray<MODE, TILT>(P, ray, label, vec, image, epa_t, epa_d, epa_r, counters);
    } else { // whole warps take part in the cooperative march
       __shared__ CoopScratch scratch[4];
-      march_ray_coop<MODE, TILT>(P, ray, ray < P.X * P.Y, label, vec, image, epa_t, epa_d,
+      march_ray_coop<MODE, TILT>(P, valid ? ray : 0, valid, label, vec, image, epa_t, epa_d,
                                  epa_r, counters, scratch[threadIdx.x >> 5]);
    }
 }
@@ -386,8 +390,11 @@ int launch_march(const MarchPlan &mp, const int32_t *d_label, const float *d_vec
    if (reinterpret_cast<uintptr_t>(d_label) % 16 || reinterpret_cast<uintptr_t>(d_vec) % 16)
       P.column = 0;
    const int64_t n_rays = P.X * P.Y;
-   const unsigned grid = (unsigned)((n_rays + 127) / 128);
    const bool tilt = P.rotate || P.dx_fx != 0 || P.dy_fx != 0;
+   const unsigned grid =
+       (!tilt && P.column)
+           ? (unsigned)((n_rays + 127) / 128)
+           : (unsigned)(((P.X + kRayTileX - 1) / kRayTileX) * ((P.Y + kRayTileY - 1) / kRayTileY));
    // separate kernels per march variant: the cooperative one holds 36 KB of
    // shared scratch and more registers, which must not cap the occupancy of
    // the per-thread one

@@ -10,7 +10,9 @@ analysis.  The server thread
   * groups admitted requests into one ``TileBatch`` (batched voxelizer + one
     persistent march over all (tile, tilt) pairs) and launches it on a free
     stream slot, so new batches start while earlier ones still run (the GPU
-    overlaps them);
+    overlaps them).  A batch of a single request goes through the plain
+    per-call kernels instead (no batch planning and upload: lower latency at
+    light load); both paths give the same bits;
   * retires finished batches (CUDA event), copies each request's epa maps to
     the host and completes it.
 
@@ -130,15 +132,18 @@ class ForwardServer:
     """Continuous batching over ``n_slots`` CUDA streams under an HBM budget."""
 
     def __init__(self, setup, hbm_budget=150e9, max_tiles=32, n_slots=2, runner=None,
-                 streams=None):
+                 streams=None, single_runner=None):
         self.budget = float(hbm_budget)
         self.max_tiles = int(max_tiles)
         self.runner = runner if runner is not None else GpuRunner(setup)
+        # batches of one request: the plain per-call path (same results)
+        self.single = single_runner if single_runner is not None else (
+            PlainRunner(setup) if runner is None else None)
         self.n_rho = self.runner.n_rho
         self._streams = streams
         self.n_slots = int(n_slots)
         self._pending = collections.deque()
-        self._inflight = []  # (handle, reqs, event, stream, nbytes)
+        self._inflight = []  # (runner, handle, reqs, event, stream, nbytes)
         self._in_bytes = 0
         self._lock = threading.Condition()
         self._run = False
@@ -191,7 +196,7 @@ class ForwardServer:
 
     # ------------------------------------------------------------ worker ---
     def _free_stream(self):
-        busy = {id(s) for _, _, _, s, _ in self._inflight}
+        busy = {id(s) for _, _, _, _, s, _ in self._inflight}
         for s in self._streams:
             if id(s) not in busy:
                 return s
@@ -208,16 +213,16 @@ class ForwardServer:
 
     def _retire(self):
         still = []
-        for h, reqs, ev, s, nb in self._inflight:
+        for run, h, reqs, ev, s, nb in self._inflight:
             if ev.query():
                 try:
-                    self.runner.collect(h, reqs, s)
+                    run.collect(h, reqs, s)
                     self._finish(reqs)
                 except Exception as e:  # noqa: BLE001 - reported per request
                     self._finish(reqs, e)
                 self._in_bytes -= nb
             else:
-                still.append((h, reqs, ev, s, nb))
+                still.append((run, h, reqs, ev, s, nb))
         self._inflight = still
 
     def _loop(self):
@@ -242,12 +247,13 @@ class ForwardServer:
                 for r in reqs:
                     r.t_start = t0
                     r.batch_size = len(reqs)
+                run = self.single if (len(reqs) == 1 and self.single is not None) else self.runner
                 try:
-                    h, ev = self.runner.launch(reqs, s)
+                    h, ev = run.launch(reqs, s)
                 except Exception as e:  # noqa: BLE001 - reported per request
                     self._finish(reqs, e)
                     continue
-                self._inflight.append((h, reqs, ev, s, nb))
+                self._inflight.append((run, h, reqs, ev, s, nb))
                 self._in_bytes += nb
                 self.batches += 1
             elif self._inflight:

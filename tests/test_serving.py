@@ -76,6 +76,25 @@ def test_server_batches_and_completes_all():
     assert len(runner.batches) < 20  # requests arriving together were batched
 
 
+def test_single_request_batches_use_the_single_runner():
+    """A batch of one request goes to the single-request runner (the plain
+    per-call path in production), larger batches to the batch runner."""
+    batch, single = FakeRunner(delay=0.05), FakeRunner(delay=0.001)
+    srv = serving.ForwardServer({"filter_rotations": np.zeros(9)}, hbm_budget=1e12,
+                                max_tiles=8, n_slots=1, runner=batch, streams=["s"],
+                                single_runner=single)
+    with srv:
+        first = srv.submit(tile(), [(0, 0)])
+        first.wait(10)
+        rest = [srv.submit(tile(), [(0, 0)]) for _ in range(6)]
+        for r in rest:
+            r.wait(10)
+    assert single.batches[0] == [first.rid]
+    assert all(len(b) == 1 for b in single.batches)
+    assert all(len(b) > 1 for b in batch.batches) and batch.batches
+    assert sum(len(b) for b in batch.batches + single.batches) == 7
+
+
 def test_budget_limits_bytes_in_flight():
     runner = FakeRunner(delay=0.03)
     t = tile()
