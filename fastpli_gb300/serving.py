@@ -31,7 +31,7 @@ import types
 
 import numpy as np
 
-_BYTES_PER_VOXEL = 4 + 12 + 8 + 4  # label, vector, key, bundle minimum
+_BYTES_PER_VOXEL = 4 + 12  # label, vector (the voxelizer keeps its keys on chip)
 
 
 def estimate_bytes(tile, tilts, n_rho, epa=True):
@@ -39,7 +39,7 @@ def estimate_bytes(tile, tilts, n_rho, epa=True):
     X, Y, Z = (int(v) for v in tile.dim)
     n_seg = sum(max(0, len(f) - 1) for b in tile.bundles for f in b)
     per_pair = X * Y * 8 * (n_rho + (3 if epa else 0)) + 1472 + 64 * 1024
-    return X * Y * Z * _BYTES_PER_VOXEL + n_seg * 256 + len(tilts) * per_pair + (1 << 20)
+    return X * Y * Z * _BYTES_PER_VOXEL + n_seg * 400 + len(tilts) * per_pair + (1 << 20)
 
 
 class Request:
