@@ -307,8 +307,12 @@ int plan_march(const fpgb_setup *s, const int64_t *dim, const double *props, int
 // ======================================================================
 // device
 // ======================================================================
+// 7 resident blocks per SM for the per-thread and column kernels (72
+// registers, a few bytes of spill: 3% faster than the 80-register default on
+// config 2; 8 blocks spill too much); the cooperative kernel keeps the 5 its
+// registers and 36 KB of shared scratch give it.
 template <int MODE, bool TILT, bool COOP>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, COOP ? 5 : 7)
 march_rays(const MarchParams P, const int32_t *__restrict__ label,
            const float *__restrict__ vec, double *__restrict__ image,
            double *__restrict__ epa_t, double *__restrict__ epa_d, double *__restrict__ epa_r,

@@ -410,8 +410,11 @@ __device__ __forceinline__ void decode_voxel(unsigned long long key, int x, int 
 }
 
 // ------------------------------------------------------------- the brick ---
+// 4 resident bricks per SM (64 registers, ~130 bytes of spill): 6% faster
+// than 3 on config 2 — the passes are latency-bound and the extra warps hide
+// more of it than the spills cost.
 template <bool MULTI>
-__global__ void __launch_bounds__(kBrickThreads, 3)
+__global__ void __launch_bounds__(kBrickThreads, 4)
 voxel_bricks(const SegDev *__restrict__ segs, const TileDev *__restrict__ tiles, int64_t n_tiles,
              int64_t n_bricks, const unsigned *__restrict__ offsets,
              const unsigned *__restrict__ list, unsigned n_pairs,
