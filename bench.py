@@ -117,22 +117,40 @@ def _peaks():
         return 6800.0, "fallback"
 
 
-def _ncu_traffic(summary):
-    """DRAM bytes (read + write) per launch of the first launch listed in a
-    committed ncu summary under profiles/ (None when absent)."""
+def _ncu_metric(summary, name):
+    """(value, unit) of a metric of the first launch in a committed ncu
+    summary under profiles/ (None when absent)."""
     import re
     try:
         text = open(os.path.join(ROOT, "profiles", summary)).read()
     except OSError:
         return None
+    m = re.search(r"`" + re.escape(name) + r"`\) \| ([0-9.]+) ?(\S*) \|", text)
+    return (float(m.group(1)), m.group(2)) if m else None
+
+
+def _ncu_traffic(summary):
+    """DRAM bytes (read + write) per launch of the first launch listed in a
+    committed ncu summary under profiles/ (None when absent)."""
     unit = {"byte": 1, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9}
-    vals = {}
+    total = 0.0
     for name in ("dram__bytes_read.sum", "dram__bytes_write.sum"):
-        m = re.search(r"`" + re.escape(name) + r"`\) \| ([0-9.]+) (\w+)", text)
-        if not m:
+        v = _ncu_metric(summary, name)
+        if v is None:
             return None
-        vals[name] = float(m.group(1)) * unit.get(m.group(2), 1)
-    return sum(vals.values())
+        total += v[0] * unit.get(v[1], 1)
+    return total
+
+
+def _ncu_limiter(summary):
+    """What bounds a kernel that is not HBM-bound, from the same summary:
+    the fraction of cycles the schedulers issued and the FMA-pipe load."""
+    issue = _ncu_metric(summary, "smsp__issue_active.avg.pct_of_peak_sustained_active")
+    fma = _ncu_metric(summary, "sm__pipe_fma_cycles_active.avg.pct_of_peak_sustained_active")
+    if issue is None:
+        return None
+    return {"kind": "instruction issue / latency (ncu)", "issue_active_frac": issue[0] / 100,
+            "fma_pipe_frac": None if fma is None else fma[0] / 100}
 
 
 # kernels of one device-resident step: the voxelizer's segment binning (count,
@@ -309,17 +327,21 @@ def run_gpu(args):
     gen_bytes = 16 * X * Y * Z
     gen_gbs = gen_bytes / (gen_avg * 1e-3) / 1e9
     if march_avg >= gen_avg:
-        traffic = _ncu_traffic("march_rays_slerp_tilted_crossing512x512x120.md")
+        prof = "march_rays_slerp_tilted_crossing512x512x120.md"
+        traffic = _ncu_traffic(prof)
         roof = {"kernel": "march_rays (5 tilts)", "bound": "hbm", "achieved": march_gbs,
                 "peak": hbm_peak, "unit": "GB/s", "frac": march_gbs / hbm_peak,
                 "traffic": traffic, "traffic_per": "one tilted launch (ncu)",
+                "limiter": _ncu_limiter(prof),
                 "algorithmic_bytes_per_launch": march_bytes / len(w.tilts),
                 "algorithmic_bytes_per_step": 16, "peak_source": peak_kind}
     else:
-        traffic = _ncu_traffic("voxel_bricks_crossing512x512x120.md")
+        prof = "voxel_bricks_crossing512x512x120.md"
+        traffic = _ncu_traffic(prof)
         roof = {"kernel": "voxel_bricks (+ binning)", "bound": "hbm", "achieved": gen_gbs,
                 "peak": hbm_peak, "unit": "GB/s", "frac": gen_gbs / hbm_peak,
                 "traffic": traffic, "traffic_per": "one launch (ncu)",
+                "limiter": _ncu_limiter(prof),
                 "algorithmic_bytes_per_launch": gen_bytes,
                 "algorithmic_bytes_per_voxel": 16, "peak_source": peak_kind}
 
