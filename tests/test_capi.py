@@ -121,3 +121,40 @@ def test_workspace_size_is_host_planned():
     g.set_volume([400, 400, 320], [0, 0, 0], 0.5)
     n_bricks = 50 * 50 * 10
     assert g.workspace_size() - ws <= 3 * 4 * n_bricks + 4096
+
+
+def test_stage_entry_points_validate_before_device_work():
+    """The optic, noise, epa and ROFL entry points refuse bad arguments with
+    FPGB_EINVAL before any CUDA call (runs without a GPU)."""
+    lib = N.load()
+    one = np.zeros(8, np.float64)
+    # sigma < 0, scale <= 0, n_rho <= 0, null buffers
+    assert lib.fpgb_optic_filter_resample_device(N.ptr(one), 2, 2, 2, -1.0, 0.5, N.ptr(one),
+                                                 None) == N.FPGB_EINVAL
+    assert lib.fpgb_optic_filter_resample_device(N.ptr(one), 2, 2, 2, 0.7, 0.0, N.ptr(one),
+                                                 None) == N.FPGB_EINVAL
+    assert lib.fpgb_optic_filter_resample_device(None, 2, 2, 2, 0.7, 0.5, N.ptr(one),
+                                                 None) == N.FPGB_EINVAL
+    assert lib.fpgb_optic_filter_resample_device(N.ptr(one), 2, 2, 0, 0.7, 0.5, N.ptr(one),
+                                                 None) == N.FPGB_EINVAL
+    # a scale that leaves no output pixel
+    assert lib.fpgb_optic_filter_resample_device(N.ptr(one), 2, 2, 2, 0.7, 0.1, N.ptr(one),
+                                                 None) == N.FPGB_EINVAL
+    assert b"empty" in lib.fpgb_last_error()
+    # noise: gain <= 1
+    assert lib.fpgb_optic_noise_device(N.ptr(one), 8, 1.0, 1, 0, N.ptr(one), None,
+                                       None) == N.FPGB_EINVAL
+    # epa: n_rho outside 1..64
+    assert lib.fpgb_epa_device(N.ptr(one), 1, 0, N.ptr(one), N.ptr(one), N.ptr(one),
+                               None) == N.FPGB_EINVAL
+    assert lib.fpgb_epa_device(N.ptr(one), 1, 65, N.ptr(one), N.ptr(one), N.ptr(one),
+                               None) == N.FPGB_EINVAL
+    # rofl: n_rot <= 3, n_rot > 32, gain <= 1
+    out = np.zeros(8)
+    assert lib.fpgb_rofl_device(N.ptr(one), 1, 3, 0.1, 3.0, 0.0, 0, None, N.ptr(out), None,
+                                None) == N.FPGB_EINVAL
+    assert lib.fpgb_rofl_device(N.ptr(one), 1, 33, 0.1, 3.0, 0.0, 0, None, N.ptr(out), None,
+                                None) == N.FPGB_EINVAL
+    assert lib.fpgb_rofl_device(N.ptr(one), 1, 6, 0.1, 1.0, 0.0, 0, None, N.ptr(out), None,
+                                None) == N.FPGB_EINVAL
+    assert b"gain" in lib.fpgb_last_error()
