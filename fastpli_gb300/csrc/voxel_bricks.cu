@@ -327,11 +327,12 @@ __device__ __forceinline__ void decode_voxel(unsigned long long key, int x, int 
                                              const SegDev *__restrict__ segs,
                                              const LayerDev *__restrict__ layers,
                                              int layer_base, int max_layer, unsigned minb,
-                                             int32_t &label_out, float o[3],
+                                             int32_t &label_out, float o[3], bool &defer,
                                              unsigned long long &n_overlap,
                                              unsigned long long &n_overflow,
                                              unsigned long long &n_slow) {
    o[0] = o[1] = o[2] = 0.f;
+   defer = false;
    if (key == ~0ull) {
       label_out = 0;
       return;
@@ -381,8 +382,10 @@ __device__ __forceinline__ void decode_voxel(unsigned long long key, int x, int 
       o[1] = S.vp[1];
       o[2] = S.vp[2];
    } else if (m == 'r') {
-      if (!evaluated)
-         evaluate();
+      if (!evaluated) { // the caller evaluates it with radial_vector, 32 at a time
+         defer = true;
+         return;
+      }
       if (!(fast && fast_radial(S, fc, o))) {
          const double pt[3] = {(double)x + 0.5, (double)y + 0.5, (double)z + 0.5};
          if (fast) {
@@ -407,6 +410,37 @@ __device__ __forceinline__ void decode_voxel(unsigned long long key, int x, int 
          o[2] = (float)nv[2];
       }
    }
+}
+
+// The 'r' orientation of voxel (x, y, z) for winner S: unit(point - closest)
+// (generator.cpp:365-371) by the two-float path, FP64 replay when undecided.
+__device__ __forceinline__ void radial_vector(const SegDev &S, int x, int y, int z, float o[3],
+                                              unsigned long long &n_slow) {
+   const float lpt[3] = {(float)(x - S.base[0]) + 0.5f, (float)(y - S.base[1]) + 0.5f,
+                         (float)(z - S.base[2]) + 0.5f};
+   FastCand fc;
+   const bool fast = S.pscale < 0x1p22f && fast_candidate(S, lpt, fc);
+   if (fast && fast_radial(S, fc, o))
+      return;
+   const double pt[3] = {(double)x + 0.5, (double)y + 0.5, (double)z + 0.5};
+   double cl[3];
+   float d_chk, r_chk;
+   exact_dist(S, pt, cl, d_chk, r_chk);
+   n_slow++;
+   double nv[3] = {pt[0] - cl[0], pt[1] - cl[1], pt[2] - cl[2]};
+   double n2 = 0.0;
+   n2 = n2 + nv[0] * nv[0];
+   n2 = n2 + nv[1] * nv[1];
+   n2 = n2 + nv[2] * nv[2];
+   if (n2 > 0) {
+      const double inv = 1.0 / sqrt(n2);
+      nv[0] = nv[0] * inv;
+      nv[1] = nv[1] * inv;
+      nv[2] = nv[2] * inv;
+   }
+   o[0] = (float)nv[0];
+   o[1] = (float)nv[1];
+   o[2] = (float)nv[2];
 }
 
 // ------------------------------------------------------------- the brick ---
@@ -494,27 +528,58 @@ voxel_bricks(const SegDev *__restrict__ segs, const TileDev *__restrict__ tiles,
                               oz, skey, sminb, n_slow);
       }
       __syncthreads();
-      // one warp per (x, y) row of the brick, lane = z: coalesced stores
+      // one warp per (x, y) row of the brick, lane = z: coalesced stores.
+      // Radial ('r') orientations of winners whose candidate the decode did
+      // not evaluate go to the warp's queue and are computed 32 at a time
+      // (a warp's row mixes 'b' and 'r' voxels: in place, half the lanes
+      // would idle through the two-float unit vector).
       int32_t *label = labels[lo];
       float *vec = vecs[lo];
+      WarpQueue &rq = queues[warp];
+      int qn = 0;
+      auto radial = [&](unsigned short li) {
+         const int rx = ox + (li >> 8), ry = oy + ((li >> 5) & 7), rz = oz + (li & 31);
+         const unsigned seg = 0xFFFFFFFFu - (unsigned)(skey[li] & 0xFFFFFFFFull);
+         float o[3];
+         radial_vector(segs[seg], rx, ry, rz, o, n_slow);
+         const int64_t i = ((int64_t)rx * Y + ry) * Z + rz;
+         vec[3 * i + 0] = o[0];
+         vec[3 * i + 1] = o[1];
+         vec[3 * i + 2] = o[2];
+      };
       for (int r = warp; r < nx * ny; r += kBrickWarps) {
          const int lx = r / ny, ly = r - (r / ny) * ny;
-         if (lane >= nz)
-            continue;
          const int li = (lx * kBrickY + ly) * kBrickZ + lane;
-         const int x = ox + lx, y = oy + ly, z = oz + lane;
-         int32_t lab;
-         float o[3];
-         decode_voxel(skey[li], x, y, z, segs, layers, layer_base, max_layer,
-                      MULTI ? sminb[li] : ~0u, lab, o, n_overlap, n_overflow, n_slow);
-         const int64_t i = ((int64_t)x * Y + y) * Z + z;
-         label[i] = lab;
-         if (vec) {
-            vec[3 * i + 0] = o[0];
-            vec[3 * i + 1] = o[1];
-            vec[3 * i + 2] = o[2];
+         bool defer = false;
+         if (lane < nz) {
+            const int x = ox + lx, y = oy + ly, z = oz + lane;
+            int32_t lab;
+            float o[3];
+            decode_voxel(skey[li], x, y, z, segs, layers, layer_base, max_layer,
+                         MULTI ? sminb[li] : ~0u, lab, o, defer, n_overlap, n_overflow, n_slow);
+            const int64_t i = ((int64_t)x * Y + y) * Z + z;
+            label[i] = lab;
+            defer = defer && vec;
+            if (vec && !defer) {
+               vec[3 * i + 0] = o[0];
+               vec[3 * i + 1] = o[1];
+               vec[3 * i + 2] = o[2];
+            }
+         }
+         const unsigned m = __ballot_sync(0xFFFFFFFFu, defer);
+         if (defer)
+            rq.entry[qn + __popc(m & ((1u << lane) - 1u))] = (unsigned short)li;
+         qn += __popc(m);
+         if (qn >= 32) {
+            __syncwarp();
+            radial(rq.entry[qn - 32 + lane]);
+            qn -= 32;
+            __syncwarp();
          }
       }
+      __syncwarp();
+      if (lane < qn)
+         radial(rq.entry[lane]);
       __syncthreads(); // shared keys are re-initialised for the next brick
    }
    if (n_overlap)
