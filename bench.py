@@ -153,6 +153,82 @@ def _ncu_limiter(summary):
             "fma_pipe_frac": None if fma is None else fma[0] / 100}
 
 
+# Per-step operation counts of the reference formulas for the march's
+# FP32 / SFU roofs (ray-voxel step with rho collapsed; background steps cost
+# one multiply): NN 50 FP32 + 4 SFU (sqrt, rcp, sin, cos); Slerp adds the 8
+# neighbour label compares and 7 interpolations of ~30 FP32 + acos + 2 sin +
+# rcp.  A vertical ray's interpolation collapses, so untilted steps count as NN.
+OPS_NN = (50, 4)
+OPS_SLERP = (50 + 8 + 7 * 30, 4 + 7 * 4)
+# voxelizer: one candidate test (a voxel of a segment's clipped box) is ~25
+# FP64 operations and one FP64 division in the reference
+FP64_PER_CANDIDATE = 26
+
+
+def measure_peaks():
+    """FP32 flop/s, SFU op/s, FP64 flop/s and L2 atomics/s of this GPU from the
+    microbenchmarks in fastpli_gb300/csrc/peaks (None if unavailable)."""
+    import ctypes
+    from fastpli_gb300 import build as fb
+    try:
+        lib = ctypes.CDLL(fb.PEAKS_LIB)
+    except OSError:
+        return None
+    lib.fpgb_measure_peaks.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    out = (ctypes.c_double * 4)()
+    if lib.fpgb_measure_peaks(out, None) != 0:
+        return None
+    return {"fp32_flops": out[0], "sfu_ops": out[1], "fp64_flops": out[2],
+            "l2_atomics": out[3]}
+
+
+def candidate_tests(w):
+    """Voxels of every segment's clipped box (generator.cpp:295-312), the
+    voxelizer's algorithmic unit, from the fiber table on the host."""
+    X, Y, Z = (int(v) for v in w.dim)
+    total = 0
+    for fibers, layers in zip(w.bundles, w.layers):
+        smax = np.sqrt(max(l[0] for l in layers) ** 2)
+        for f in fibers:
+            p = (np.asarray(f[:, :3], np.float64) - np.asarray(w.origin)) * (1.0 / w.voxel_size)
+            r = np.asarray(f[:, 3], np.float64) * (1.0 / w.voxel_size)
+            rmax = np.maximum(r[:-1], r[1:]) * smax
+            lo = np.minimum(p[:-1], p[1:]) - rmax[:, None]
+            hi = np.maximum(p[:-1], p[1:]) + rmax[:, None]
+            lo = np.clip(lo, 0, [X, Y, Z])
+            hi = np.clip(hi, 0, [X, Y, Z])
+            ext = np.maximum(np.floor(hi + 0.5) - np.trunc(lo), 0)
+            total += int(np.prod(ext, axis=1).sum())
+    return total
+
+
+def roofline_model(peaks, hbm_gbs, w, n_steps_untilted, n_steps_tilted, tissue_frac,
+                   march_steps_per_s, candidates, voxelize_s):
+    """The march against min(HBM, FP32, SFU) steps/s and the voxelizer against
+    the FP64 rate at the reference's per-candidate work."""
+    if peaks is None:
+        return None
+    f = tissue_frac
+    fp32 = ((f * OPS_NN[0] + 1 - f) * n_steps_untilted +
+            (f * OPS_SLERP[0] + 1 - f) * n_steps_tilted) / (n_steps_untilted + n_steps_tilted)
+    sfu = (f * OPS_NN[1] * n_steps_untilted + f * OPS_SLERP[1] * n_steps_tilted) / (
+        n_steps_untilted + n_steps_tilted)
+    roofs = {"hbm": hbm_gbs * 1e9 / 16, "fp32": peaks["fp32_flops"] / fp32,
+             "sfu": peaks["sfu_ops"] / sfu}
+    bound = min(roofs, key=roofs.get)
+    vox_roof = peaks["fp64_flops"] / FP64_PER_CANDIDATE
+    vox_rate = candidates / voxelize_s
+    return {
+        "measured_peaks": peaks,
+        "march": {"unit": "ray-voxel steps/s", "achieved": march_steps_per_s,
+                  "roofs": roofs, "bound": bound, "frac": march_steps_per_s / roofs[bound],
+                  "ops_per_step": {"fp32": fp32, "sfu": sfu}, "tissue_step_frac": f},
+        "voxelizer": {"unit": "candidate tests/s", "achieved": vox_rate,
+                      "candidates": candidates, "roof_fp64": vox_roof, "bound": "fp64",
+                      "frac": vox_rate / vox_roof},
+    }
+
+
 # kernels of one device-resident step: the voxelizer's segment binning (count,
 # scan, fill) and brick kernel, then one march per tilt
 VOXELIZER_LAUNCHES = 4
@@ -319,6 +395,11 @@ def run_gpu(args):
     hbm_peak, peak_kind = _peaks()
     gen_avg = sum(gen_ms) / len(gen_ms)
     march_avg = sum(march_ms) / len(march_ms)
+    n_untilted = sum(sim.count_steps(w.dim, float(t), float(p))
+                     for t, p in w.tilts if float(t) == 0.0)
+    model = roofline_model(measure_peaks(), hbm_peak, w, n_untilted, steps_per - n_untilted,
+                           tissue_voxels / float(X * Y * Z), steps_per / (march_avg * 1e-3),
+                           candidate_tests(w), gen_avg * 1e-3)
     # march: one label (4 B) and one axis (12 B) per ray-voxel step
     march_bytes = 16 * steps_per
     march_gbs = march_bytes / (march_avg * 1e-3) / 1e9
@@ -364,7 +445,7 @@ def run_gpu(args):
             "tissue_voxels_per_s": tissue_voxels / (gen_avg * 1e-3),
             "voxelize_ms": gen_avg, "march_ms": march_avg,
             "march_steps_per_s": steps_per / (march_avg * 1e-3),
-            "roofline": roof, "cpu_baseline": cpu,
+            "roofline": roof, "roofline_model": model, "cpu_baseline": cpu,
             "e2e": {"value": ws * steps_per / e2e_s, "unit": UNIT,
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": args.steps * (VOXELIZER_LAUNCHES + len(w.tilts)),

@@ -31,6 +31,9 @@ OUT_DIR = os.path.join(HERE, "_lib")
 OBJ_DIR = os.path.join(HERE, "_lib", "obj")
 LIB_NAME = "libfastpli_gb300.so"
 LIB_PATH = os.path.join(OUT_DIR, LIB_NAME)
+# throughput microbenchmarks for the roofline (bench.py), outside the path's ABI
+PEAKS_SRC = os.path.join(CSRC, "peaks", "peaks.cu")
+PEAKS_LIB = os.path.join(OUT_DIR, "libfpgb_peaks.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
@@ -65,10 +68,10 @@ def _compile(nvcc, src, extra):
 
 
 def _stale():
-    if not os.path.exists(LIB_PATH):
+    if not os.path.exists(LIB_PATH) or not os.path.exists(PEAKS_LIB):
         return True
     t = os.path.getmtime(LIB_PATH)
-    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
+    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [PEAKS_SRC]
     deps += [os.path.join(ROOT, "include", f) for f in os.listdir(os.path.join(ROOT, "include"))]
     deps.append(__file__)
     return any(os.path.getmtime(d) > t for d in deps)
@@ -81,8 +84,16 @@ def build(force=False, verbose=False, extra=()):
     nvcc = _nvcc()
     os.makedirs(OBJ_DIR, exist_ok=True)
     extra = list(extra)
+    def peaks():
+        r = subprocess.run([nvcc, *ARCH, *COMMON, "-shared", PEAKS_SRC, "-o", PEAKS_LIB],
+                           capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed on peaks.cu:\n{r.stdout}\n{r.stderr}")
+
     with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 1)) as ex:
+        peaks_job = ex.submit(peaks)
         results = list(ex.map(lambda s: _compile(nvcc, s, extra), sources()))
+        peaks_job.result()
     objs = [o for o, _ in results]
     if verbose:
         for _, err in results:
