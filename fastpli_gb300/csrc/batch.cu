@@ -70,6 +70,7 @@ struct fpgb_batch_impl {
    int64_t n_untilted = 0; // items [0, n_untilted) untilted, the rest tilted
    int sms = 1;
    int fit[2][2] = {{1, 1}, {1, 1}}; // resident CTAs per SM: [untilted / tilted][per-thread / coop]
+   bool narrow = true; // every (tile, tilt) pair allows 32-bit index arithmetic
 };
 
 // ----------------------------------------------------------------------------
@@ -81,7 +82,7 @@ struct fpgb_batch_impl {
 static_assert(sizeof(MarchParams) % 16 == 0, "MarchParams is copied as int4");
 constexpr int kBatchThreads = 128; // one work item = one CTA-width block of rays
 
-template <int MODE, bool TILT, bool COOP>
+template <int MODE, bool TILT, bool COOP, bool WIDE>
 __global__ void __launch_bounds__(128)
 batch_march(const MarchParams *__restrict__ prm, const BatchItem *__restrict__ items,
             int64_t n_items, int chunk, unsigned long long *__restrict__ next,
@@ -120,10 +121,10 @@ batch_march(const MarchParams *__restrict__ prm, const BatchItem *__restrict__ i
                                     sP.epa_r, counters);
          } else if (MODE == 0 || !COOP) {
             if (valid)
-               march_one_ray<MODE, TILT>(sP, ray, sP.label, sP.vec, sP.image, sP.epa_t,
+               march_one_ray<MODE, TILT, WIDE>(sP, ray, sP.label, sP.vec, sP.image, sP.epa_t,
                                          sP.epa_d, sP.epa_r, counters);
          } else {
-            march_ray_coop<MODE, TILT>(sP, ray, valid, sP.label, sP.vec, sP.image, sP.epa_t,
+            march_ray_coop<MODE, TILT, WIDE>(sP, ray, valid, sP.label, sP.vec, sP.image, sP.epa_t,
                                        sP.epa_d, sP.epa_r, counters, scratch[threadIdx.x >> 5]);
          }
       }
@@ -131,31 +132,47 @@ batch_march(const MarchParams *__restrict__ prm, const BatchItem *__restrict__ i
    }
 }
 
-template <int MODE, bool TILT>
-int batch_march_fit(int fit[2]) {
+template <int MODE, bool TILT, bool WIDE>
+int batch_march_fit_w(int fit[2]) {
    FPGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-       &fit[0], batch_march<MODE, TILT, false>, kBatchThreads, 0));
+       &fit[0], batch_march<MODE, TILT, false, WIDE>, kBatchThreads, 0));
    FPGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-       &fit[1], batch_march<MODE, TILT, true>, kBatchThreads, 0));
+       &fit[1], batch_march<MODE, TILT, true, WIDE>, kBatchThreads, 0));
    return FPGB_OK;
+}
+
+template <int MODE, bool TILT>
+int batch_march_fit(int fit[2], bool narrow) {
+   return narrow ? batch_march_fit_w<MODE, TILT, false>(fit)
+                 : batch_march_fit_w<MODE, TILT, true>(fit);
 }
 
 template <int MODE, bool TILT>
 int launch_batch_march(const MarchParams *prm, const BatchItem *items, int64_t n_items,
                        unsigned long long *next, unsigned long long *counters, int sms,
-                       const int fits[2], int ctas_per_sm, int chunk, int coop, cudaStream_t st) {
+                       const int fits[2], int ctas_per_sm, int chunk, int coop, bool narrow,
+                       cudaStream_t st) {
    if (n_items <= 0)
       return FPGB_OK;
    const bool cp = MODE != 0 && coop != 0;
    const int fit = fits[cp ? 1 : 0];
    const int per_sm = std::max(1, std::min(ctas_per_sm > 0 ? ctas_per_sm : fit, fit));
    const int64_t grid = std::min<int64_t>((int64_t)sms * per_sm, (n_items + chunk - 1) / chunk);
-   if (cp)
-      batch_march<MODE, TILT, true><<<(unsigned)grid, kBatchThreads, 0, st>>>(
-          prm, items, n_items, chunk, next, counters);
-   else
-      batch_march<MODE, TILT, false><<<(unsigned)grid, kBatchThreads, 0, st>>>(
-          prm, items, n_items, chunk, next, counters);
+#define FPGB_BM(C, W)                                                                         \
+   batch_march<MODE, TILT, C, W><<<(unsigned)grid, kBatchThreads, 0, st>>>(prm, items, n_items, \
+                                                                           chunk, next, counters)
+   if (cp) {
+      if (narrow)
+         FPGB_BM(true, false);
+      else
+         FPGB_BM(true, true);
+   } else {
+      if (narrow)
+         FPGB_BM(false, false);
+      else
+         FPGB_BM(false, true);
+   }
+#undef FPGB_BM
    FPGB_CUDA_TRY(cudaGetLastError());
    return FPGB_OK;
 }
@@ -252,6 +269,7 @@ int plan_batch(int64_t n_tiles, const fpgb_volume *vols, const fpgb_fibers *fibe
                              tilts[2 * k], tilts[2 * k + 1], &mp));
          mp.prm.tilted = (mp.prm.rotate || mp.prm.dx_fx != 0 || mp.prm.dy_fx != 0) ? 1 : 0;
          B->steps += mp.steps;
+         B->narrow = B->narrow && march_narrow(mp.prm);
          B->pairs.push_back(std::move(mp));
          B->pair_tile.push_back((int32_t)t);
       }
@@ -381,16 +399,16 @@ int upload_batch(fpgb_batch_impl *B, void *arena, void *ws, cudaStream_t st) {
    B->sms = sm_count_now();
    switch (B->setup.interpolate) {
    case 0:
-      FPGB_TRY((batch_march_fit<0, false>(B->fit[0])));
-      FPGB_TRY((batch_march_fit<0, true>(B->fit[1])));
+      FPGB_TRY((batch_march_fit<0, false>(B->fit[0], B->narrow)));
+      FPGB_TRY((batch_march_fit<0, true>(B->fit[1], B->narrow)));
       break;
    case 1:
-      FPGB_TRY((batch_march_fit<1, false>(B->fit[0])));
-      FPGB_TRY((batch_march_fit<1, true>(B->fit[1])));
+      FPGB_TRY((batch_march_fit<1, false>(B->fit[0], B->narrow)));
+      FPGB_TRY((batch_march_fit<1, true>(B->fit[1], B->narrow)));
       break;
    default:
-      FPGB_TRY((batch_march_fit<2, false>(B->fit[0])));
-      FPGB_TRY((batch_march_fit<2, true>(B->fit[1])));
+      FPGB_TRY((batch_march_fit<2, false>(B->fit[0], B->narrow)));
+      FPGB_TRY((batch_march_fit<2, true>(B->fit[1], B->narrow)));
       break;
    }
    return FPGB_OK;
@@ -427,9 +445,9 @@ int run_batch(fpgb_batch_impl *B, int march_ctas_per_sm, int chunk, int coop, cu
    const int ch = chunk > 0 ? chunk : 4;
 #define FPGB_BATCH_MARCH(M)                                                                    \
    FPGB_TRY((launch_batch_march<M, false>(prm, items, n0, next, counters, B->sms, B->fit[0],   \
-                                          march_ctas_per_sm, ch, coop, st)));                        \
+                                          march_ctas_per_sm, ch, coop, B->narrow, st)));            \
    FPGB_TRY((launch_batch_march<M, true>(prm, items + n0, n1, next + 1, counters, B->sms,      \
-                                         B->fit[1], march_ctas_per_sm, ch, coop, st)))
+                                         B->fit[1], march_ctas_per_sm, ch, coop, B->narrow, st)))
    switch (B->setup.interpolate) {
    case 0: FPGB_BATCH_MARCH(0); break;
    case 1: FPGB_BATCH_MARCH(1); break;

@@ -27,7 +27,8 @@ __device__ __forceinline__ float dot3(F3 a, F3 b) {
    return fmaf(a.z, b.z, fmaf(a.y, b.y, a.x * b.x));
 }
 
-__device__ __forceinline__ F3 load_vec(const float *__restrict__ vec, int64_t idx) {
+template <typename U>
+__device__ __forceinline__ F3 load_vec(const float *__restrict__ vec, U idx) {
    const float *p = vec + 3 * idx;
    return F3{__ldg(p), __ldg(p + 1), __ldg(p + 2)};
 }
@@ -98,38 +99,85 @@ __device__ __forceinline__ F3 interp_axis(F3 v, F3 u, float t) {
    return slerp_axis(v, u, t);
 }
 
-__device__ __forceinline__ int64_t clampi(int64_t v, int64_t hi) {
-   return v < 0 ? 0 : (v > hi ? hi : v);
+// Index arithmetic of the march.  Narrow (WIDE = false): coordinates in
+// 32-bit integers and the linear voxel index in unsigned 32 bits, for volumes
+// with 3 X Y Z < 2^32 whose fixed-point format has frac_bits >= 32 (ray
+// positions below 2^30 voxels; march_narrow picks it).  Wide: 64 bits
+// throughout.  Both give the same bits.
+template <bool WIDE> struct MarchIdx {
+   using C = int64_t; // coordinate
+   using U = int64_t; // linear voxel index
+};
+template <> struct MarchIdx<false> {
+   using C = int32_t;
+   using U = uint32_t;
+};
+
+// floor(p / 2^F) of a fixed-point position
+template <bool WIDE>
+__device__ __forceinline__ typename MarchIdx<WIDE>::C fx_floor(int64_t p, int F) {
+   if constexpr (WIDE)
+      return p >> F;
+   else
+      return (int32_t)(p >> 32) >> (F - 32); // F >= 32: one shift of the high word
+}
+
+// The fraction of a fixed-point position, truncated to 23 bits and built
+// from its bits: exact, no conversion instruction (absolute error < 2^-23,
+// far below the image tolerance).  Needs F >= 24.
+__device__ __forceinline__ float fx_frac(int64_t p, int F) {
+   const uint32_t m = (uint32_t)((uint64_t)p >> (F - 23)) & 0x7FFFFFu;
+   return __uint_as_float(0x3F800000u | m) - 1.f;
+}
+
+// Whether the position has a nonzero fraction (llceil != llfloor).
+__device__ __forceinline__ bool fx_has_frac(int64_t p, int F) {
+   return ((uint64_t)p << (64 - F)) != 0;
+}
+
+template <typename C> __device__ __forceinline__ C clampc(C v, C hi) {
+   return v < 0 ? C(0) : (v > hi ? hi : v);
+}
+
+// Linear index (x * Y + y) * Z + z of voxel (x, y, z).
+template <bool WIDE>
+__device__ __forceinline__ typename MarchIdx<WIDE>::U
+voxel_index(const MarchParams &P, typename MarchIdx<WIDE>::C x, typename MarchIdx<WIDE>::C y,
+            typename MarchIdx<WIDE>::C z) {
+   using U = typename MarchIdx<WIDE>::U;
+   return ((U)x * (U)P.Y + (U)y) * (U)P.Z + (U)z;
 }
 
 // Trilinear axis interpolation over same-label neighbours
-// (simulator.cpp:496-555).  fx, fy: fixed-point positions of the ray.
-template <int MODE>
+// (simulator.cpp:496-555).  px, py: fixed-point positions of the ray.
+template <int MODE, bool WIDE>
 __device__ F3 axis_interp(const MarchParams &P, const int32_t *__restrict__ label,
                           const float *__restrict__ vec, int64_t px, int64_t py,
                           const ZStep &zs, int lab) {
+   using C = typename MarchIdx<WIDE>::C;
+   using U = typename MarchIdx<WIDE>::U;
    const int F = P.frac_bits;
    const int64_t half = int64_t(1) << (F - 1);
    const int64_t hx = px - half, hy = py - half;
-   const int64_t fx0 = hx >> F, fy0 = hy >> F;
-   const uint64_t mask = (uint64_t(1) << F) - 1;
-   const float scale = __int_as_float((127 - F) << 23); // 2^-F
-   const float xf = (float)(int64_t)((uint64_t)hx & mask) * scale;
-   const float yf = (float)(int64_t)((uint64_t)hy & mask) * scale;
-   const int64_t x0 = clampi(fx0, P.X - 1), x1 = clampi(fx0 + (xf != 0.f), P.X - 1);
-   const int64_t y0 = clampi(fy0, P.Y - 1), y1 = clampi(fy0 + (yf != 0.f), P.Y - 1);
-   int64_t z0 = clampi(zs.z0, P.Z - 1), z1 = clampi((int64_t)zs.z0 + (zs.zf != 0.f), P.Z - 1);
-   const float xd = (x0 != x1) ? xf : 0.f;
-   const float yd = (y0 != y1) ? yf : 0.f;
-   const float zd = (z0 != z1) ? zs.zf : 0.f;
-   if (P.flip_z) {
-      z0 = P.Z - 1 - z0;
-      z1 = P.Z - 1 - z1;
-   }
-   const int64_t YZ = P.Y * P.Z;
+   const C fx0 = fx_floor<WIDE>(hx, F), fy0 = fx_floor<WIDE>(hy, F);
+   const C xm = (C)P.X - 1, ym = (C)P.Y - 1, zm = (C)P.Z - 1;
+   const C x0 = clampc<C>(fx0, xm), x1 = clampc<C>(fx0 + (C)fx_has_frac(hx, F), xm);
+   const C y0 = clampc<C>(fy0, ym), y1 = clampc<C>(fy0 + (C)fx_has_frac(hy, F), ym);
+   C z0 = clampc<C>((C)zs.z0, zm), z1 = clampc<C>((C)zs.z0 + (C)(zs.zf != 0.f), zm);
    const bool ax = x0 != x1, ay = y0 != y1, az = z0 != z1;
+   const float xd = ax ? fx_frac(hx, F) : 0.f;
+   const float yd = ay ? fx_frac(hy, F) : 0.f;
+   const float zd = az ? zs.zf : 0.f;
+   if (P.flip_z) {
+      z0 = zm - z0;
+      z1 = zm - z1;
+   }
+   const U base = voxel_index<WIDE>(P, x0, y0, z0);
    if (!ax && !ay && !az)
-      return load_vec(vec, x0 * YZ + y0 * P.Z + z0);
+      return load_vec(vec, base);
+   // corner offsets along each axis (the z one is negative when mirrored;
+   // unsigned wrap-around then still lands on the right index)
+   const U ox = (U)(x1 - x0) * (U)P.Y * (U)P.Z, oy = (U)(y1 - y0) * (U)P.Z, oz = (U)(z1 - z0);
    // Corners along a collapsed axis coincide, and interpolating a vector
    // with itself returns it unchanged (both the reference's Lerp and Slerp),
    // so collapsed levels are skipped without changing the result.
@@ -138,8 +186,7 @@ __device__ F3 axis_interp(const MarchParams &P, const int32_t *__restrict__ labe
    for (int k = 0; k < 8; k++) {
       if (((k & 1) && !ax) || ((k & 2) && !ay) || ((k & 4) && !az))
          continue;
-      const int64_t xi = (k & 1) ? x1 : x0, yi = (k & 2) ? y1 : y0, zi = (k & 4) ? z1 : z0;
-      const int64_t idx = xi * YZ + yi * P.Z + zi;
+      const U idx = base + ((k & 1) ? ox : U(0)) + ((k & 2) ? oy : U(0)) + ((k & 4) ? oz : U(0));
       // GetVec(...) * (GetLabel(...) == label) (simulator.cpp:533-540)
       const float m = (__ldg(label + idx) == lab) ? 1.f : 0.f;
       const F3 u = load_vec(vec, idx);
@@ -359,7 +406,7 @@ __device__ __forceinline__ void apply_retard(float &u1, float &u2, float &u3, fl
 
 // One CCD-pixel ray, one thread, every step in order.  Used for NN, where a
 // birefringent step costs one vector load.
-template <int MODE, bool TILT>
+template <int MODE, bool TILT, bool WIDE>
 __device__ __forceinline__ void march_one_ray(const MarchParams &P, int64_t ray,
                                               const int32_t *__restrict__ label,
                                               const float *__restrict__ vec,
@@ -368,27 +415,29 @@ __device__ __forceinline__ void march_one_ray(const MarchParams &P, int64_t ray,
                                               double *__restrict__ epa_d,
                                               double *__restrict__ epa_r,
                                               unsigned long long *__restrict__ counters) {
+   using C = typename MarchIdx<WIDE>::C;
+   using U = typename MarchIdx<WIDE>::U;
    const int F = P.frac_bits;
    int64_t px, py;
    ray_setup(P, ray, px, py);
-   const int64_t YZ = P.Y * P.Z;
    float u1 = 0.f, u2 = 0.f, u3 = -1.f, L = 0.f;
    bool w_zero = false, w_norm = false, bad_label = false;
-   int64_t ix = px >> F, iy = py >> F;
-   bool inside = ix >= 0 && ix < P.X && iy >= 0 && iy < P.Y;
+   const C X = (C)P.X, Y = (C)P.Y;
+   C ix = fx_floor<WIDE>(px, F), iy = fx_floor<WIDE>(py, F);
+   bool inside = ix >= 0 && ix < X && iy >= 0 && iy < Y;
    for (int k = 0; k < P.n_z; k++) {
       if (TILT && k > 0) {
          px += P.dx_fx;
          py += P.dy_fx;
-         ix = px >> F;
-         iy = py >> F;
-         inside = ix >= 0 && ix < P.X && iy >= 0 && iy < P.Y;
+         ix = fx_floor<WIDE>(px, F);
+         iy = fx_floor<WIDE>(py, F);
+         inside = ix >= 0 && ix < X && iy >= 0 && iy < Y;
       }
       const ZStep zs = P.ztab[k];
       int lab = 0;
-      int64_t idx = 0;
+      U idx = 0;
       if (inside) {
-         idx = ix * YZ + iy * P.Z + zs.iz;
+         idx = voxel_index<WIDE>(P, ix, iy, (C)zs.iz);
          lab = __ldg(label + idx);
          if (lab < 0 || lab >= P.n_props) {
             bad_label = true;
@@ -406,7 +455,7 @@ __device__ __forceinline__ void march_one_ray(const MarchParams &P, int64_t ray,
       if (MODE == 0)
          v = load_vec(vec, idx);
       else
-         v = axis_interp<MODE>(P, label, vec, px, py, zs, lab);
+         v = axis_interp<MODE, WIDE>(P, label, vec, px, py, zs, lab);
       if (is_zero(v)) { // simulator.cpp:292-297: no attenuation either
          w_zero = true;
          continue;
@@ -552,7 +601,7 @@ __device__ __noinline__ F3 interp_axis_call(F3 v, F3 u, float t) {
    return interp_axis<MODE>(v, u, t);
 }
 
-template <int MODE, bool TILT>
+template <int MODE, bool TILT, bool WIDE>
 __device__ __forceinline__ void coop_job(const MarchParams &P, const int32_t *__restrict__ label,
                                          const float *__restrict__ vec, CoopScratch &S,
                                          int slot) {
@@ -563,19 +612,22 @@ __device__ __forceinline__ void coop_job(const MarchParams &P, const int32_t *__
    const float xd = S.f[4][slot], yd = S.f[5][slot], zd = S.f[6][slot];
    const int lab = __float_as_int(S.f[7][slot]);
    const bool ax = fl & 1, ay = fl & 2, az = fl & 4;
-   const int z1 = z0 + ((fl >> 3) & 3) - 1;
-   const int64_t YZ = P.Y * P.Z;
+   using C = typename MarchIdx<WIDE>::C;
+   using U = typename MarchIdx<WIDE>::U;
+   const int dz = ((fl >> 3) & 3) - 1; // z1 - z0
+   const U base = voxel_index<WIDE>(P, (C)x0, (C)y0, (C)z0);
    F3 v;
    if (!ax && !ay && !az) {
-      v = load_vec(vec, (int64_t)x0 * YZ + (int64_t)y0 * P.Z + z0);
+      v = load_vec(vec, base);
    } else {
+      const U ox = (U)P.Y * (U)P.Z, oy = (U)P.Z, oz = (U)(C)dz;
       F3 c[8];
 #pragma unroll
       for (int k = 0; k < 8; k++) {
          if (((k & 1) && !ax) || ((k & 2) && !ay) || ((k & 4) && !az))
             continue;
-         const int xi = x0 + (k & 1), yi = y0 + ((k >> 1) & 1), zi = (k & 4) ? z1 : z0;
-         const int64_t idx = (int64_t)xi * YZ + (int64_t)yi * P.Z + zi;
+         const U idx =
+             base + ((k & 1) ? ox : U(0)) + ((k & 2) ? oy : U(0)) + ((k & 4) ? oz : U(0));
          // GetVec(...) * (GetLabel(...) == label) (simulator.cpp:533-540);
          // label and axis loads are issued together
          const float m = (__ldg(label + idx) == lab) ? 1.f : 0.f;
@@ -623,7 +675,7 @@ __device__ __forceinline__ void coop_job(const MarchParams &P, const int32_t *__
    S.f[4][slot] = __int_as_float(status);
 }
 
-template <int MODE, bool TILT>
+template <int MODE, bool TILT, bool WIDE>
 __device__ __forceinline__ void march_ray_coop(const MarchParams &P, int64_t ray, bool active,
                                                const int32_t *__restrict__ label,
                                                const float *__restrict__ vec,
@@ -633,15 +685,14 @@ __device__ __forceinline__ void march_ray_coop(const MarchParams &P, int64_t ray
                                                double *__restrict__ epa_r,
                                                unsigned long long *__restrict__ counters,
                                                CoopScratch &S) {
+   using C = typename MarchIdx<WIDE>::C;
    const int lane = threadIdx.x & 31;
    const int F = P.frac_bits;
-   const int64_t YZ = P.Y * P.Z;
    int64_t px = 0, py = 0;
    if (active)
       ray_setup(P, ray, px, py);
    const int64_t half = int64_t(1) << (F - 1);
-   const uint64_t mask = (uint64_t(1) << F) - 1;
-   const float scale = __int_as_float((127 - F) << 23); // 2^-F
+   const C xm = (C)P.X - 1, ym = (C)P.Y - 1, zm = (C)P.Z - 1;
    float u1 = 0.f, u2 = 0.f, u3 = -1.f, L = 0.f;
    bool w_zero = false, w_norm = false, bad_label = false;
    for (int k0 = 0; k0 < P.n_z; k0 += kCoopSteps) {
@@ -658,11 +709,11 @@ __device__ __forceinline__ void march_ray_coop(const MarchParams &P, int64_t ray
             px += P.dx_fx;
             py += P.dy_fx;
          }
-         const int64_t ix = px >> F, iy = py >> F;
+         const C ix = fx_floor<WIDE>(px, F), iy = fx_floor<WIDE>(py, F);
          const ZStep zs = P.ztab[k];
          int lab = 0;
-         if (ix >= 0 && ix < P.X && iy >= 0 && iy < P.Y) {
-            lab = __ldg(label + ix * YZ + iy * P.Z + zs.iz);
+         if (ix >= 0 && ix <= xm && iy >= 0 && iy <= ym) {
+            lab = __ldg(label + voxel_index<WIDE>(P, ix, iy, (C)zs.iz));
             if (lab < 0 || lab >= P.n_props) {
                bad_label = true;
                lab = 0;
@@ -675,25 +726,25 @@ __device__ __forceinline__ void march_ray_coop(const MarchParams &P, int64_t ray
             continue;
          // trilinear corners as in axis_interp (simulator.cpp:510-530)
          const int64_t hx = px - half, hy = py - half;
-         const int64_t fx0 = hx >> F, fy0 = hy >> F;
-         const float xf = (float)(int64_t)((uint64_t)hx & mask) * scale;
-         const float yf = (float)(int64_t)((uint64_t)hy & mask) * scale;
-         const int64_t x0 = clampi(fx0, P.X - 1), x1 = clampi(fx0 + (xf != 0.f), P.X - 1);
-         const int64_t y0 = clampi(fy0, P.Y - 1), y1 = clampi(fy0 + (yf != 0.f), P.Y - 1);
-         int64_t z0 = clampi(zs.z0, P.Z - 1), z1 = clampi((int64_t)zs.z0 + (zs.zf != 0.f), P.Z - 1);
-         const float zd = (z0 != z1) ? zs.zf : 0.f;
-         if (P.flip_z) {
-            z0 = P.Z - 1 - z0;
-            z1 = P.Z - 1 - z1;
-         }
+         const C fx0 = fx_floor<WIDE>(hx, F), fy0 = fx_floor<WIDE>(hy, F);
+         const C x0 = clampc<C>(fx0, xm), x1 = clampc<C>(fx0 + (C)fx_has_frac(hx, F), xm);
+         const C y0 = clampc<C>(fy0, ym), y1 = clampc<C>(fy0 + (C)fx_has_frac(hy, F), ym);
+         C z0 = clampc<C>((C)zs.z0, zm), z1 = clampc<C>((C)zs.z0 + (C)(zs.zf != 0.f), zm);
          const int ax = x0 != x1, ay = y0 != y1, az = z0 != z1;
+         const float xf = ax ? fx_frac(hx, F) : 0.f;
+         const float yf = ay ? fx_frac(hy, F) : 0.f;
+         const float zd = az ? zs.zf : 0.f;
+         if (P.flip_z) {
+            z0 = zm - z0;
+            z1 = zm - z1;
+         }
          const int slot = j * 32 + lane;
          S.f[0][slot] = __int_as_float((int)x0);
          S.f[1][slot] = __int_as_float((int)y0);
          S.f[2][slot] = __int_as_float((int)z0);
          S.f[3][slot] = __int_as_float(ax | (ay << 1) | (az << 2) | ((int)(z1 - z0 + 1) << 3));
-         S.f[4][slot] = ax ? xf : 0.f;
-         S.f[5][slot] = ay ? yf : 0.f;
+         S.f[4][slot] = xf;
+         S.f[5][slot] = yf;
          S.f[6][slot] = zd;
          S.f[7][slot] = __int_as_float(lab);
       }
@@ -718,7 +769,7 @@ __device__ __forceinline__ void march_ray_coop(const MarchParams &P, int64_t ray
       }
       __syncwarp();
       for (int t = lane; t < total; t += 32)
-         coop_job<MODE, TILT>(P, label, vec, S, S.list[t]);
+         coop_job<MODE, TILT, WIDE>(P, label, vec, S, S.list[t]);
       __syncwarp();
       // phase 3: apply this lane's steps in order
 #pragma unroll

@@ -311,7 +311,7 @@ int plan_march(const fpgb_setup *s, const int64_t *dim, const double *props, int
 // registers, a few bytes of spill: 3% faster than the 80-register default on
 // config 2; 8 blocks spill too much); the cooperative kernel keeps the 5 its
 // registers and 36 KB of shared scratch give it.
-template <int MODE, bool TILT, bool COOP>
+template <int MODE, bool TILT, bool COOP, bool WIDE>
 __global__ void __launch_bounds__(128, COOP ? 5 : 7)
 march_rays(const MarchParams P, const int32_t *__restrict__ label,
            const float *__restrict__ vec, double *__restrict__ image,
@@ -327,10 +327,11 @@ march_rays(const MarchParams P, const int32_t *__restrict__ label,
    const bool valid = tile_ray<MODE != 0 && COOP>(P, blockIdx.x, threadIdx.x, ray);
    if (MODE == 0 || !COOP) {
       if (valid)
-         march_one_ray<MODE, TILT>(P, ray, label, vec, image, epa_t, epa_d, epa_r, counters);
+         march_one_ray<MODE, TILT, WIDE>(P, ray, label, vec, image, epa_t, epa_d, epa_r,
+                                         counters);
    } else { // whole warps take part in the cooperative march
       __shared__ CoopScratch scratch[4];
-      march_ray_coop<MODE, TILT>(P, valid ? ray : 0, valid, label, vec, image, epa_t, epa_d,
+      march_ray_coop<MODE, TILT, WIDE>(P, valid ? ray : 0, valid, label, vec, image, epa_t, epa_d,
                                  epa_r, counters, scratch[threadIdx.x >> 5]);
    }
 }
@@ -403,9 +404,14 @@ int launch_march(const MarchPlan &mp, const int32_t *d_label, const float *d_vec
    // shared scratch and more registers, which must not cap the occupancy of
    // the per-thread one
 #define FPGB_LAUNCH(M, T, C)                                                               \
-   march_rays<M, T, C><<<grid, 128, 0, st>>>(P, d_label, d_vec, d_image, d_t, d_d, d_r,      \
-                                             d_counters)
+   if (narrow)                                                                              \
+      march_rays<M, T, C, false><<<grid, 128, 0, st>>>(P, d_label, d_vec, d_image, d_t, d_d, \
+                                                       d_r, d_counters);                     \
+   else                                                                                     \
+      march_rays<M, T, C, true><<<grid, 128, 0, st>>>(P, d_label, d_vec, d_image, d_t, d_d,  \
+                                                      d_r, d_counters)
    const bool coop = P.coop != 0;
+   const bool narrow = march_narrow(P);
    switch (P.mode * 4 + (tilt ? 2 : 0) + (coop ? 1 : 0)) {
    case 0: case 1: FPGB_LAUNCH(0, false, false); break;
    case 2: case 3: FPGB_LAUNCH(0, true, false); break;

@@ -69,6 +69,13 @@ struct MarchPlan {
    int64_t steps; // X*Y*n_z
 };
 
+// Whether the march may use 32-bit index arithmetic (MarchIdx<false>):
+// 3 X Y Z < 2^32 and ray positions below 2^30 voxels (frac_bits >= 32).
+inline bool march_narrow(const MarchParams &P) {
+   return P.frac_bits >= 32 && P.X > 0 && P.Y > 0 && P.Z > 0 &&
+          (double)P.X * (double)P.Y * (double)P.Z * 3.0 < 4294967296.0;
+}
+
 int plan_march(const fpgb_setup *setup, const int64_t *dim, const double *props,
                int64_t n_props, double theta, double phi, MarchPlan *plan);
 
