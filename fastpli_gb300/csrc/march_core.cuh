@@ -48,47 +48,60 @@ __device__ __forceinline__ F3 lerp_axis(F3 v, F3 u, float t) {
 }
 
 // sin(sqrt(y)) / sqrt(y) by its Taylor series in y = x^2, truncated after
-// y^5 (remainder < y^6 / 13! <= 4e-13 for y <= 0.36)
+// y^4 (remainder < y^5 / 11! <= 1.6e-10 for y <= 0.36)
 __device__ __forceinline__ float sinc_sq(float y) {
-   float p = -1.f / 39916800.f;
-   p = fmaf(p, y, 1.f / 362880.f);
+   float p = 1.f / 362880.f;
    p = fmaf(p, y, -1.f / 5040.f);
    p = fmaf(p, y, 1.f / 120.f);
    p = fmaf(p, y, -1.f / 6.f);
    return fmaf(p, y, 1.f);
 }
 
+// acos(1 - x)^2 for x = 1 - cos(th) in [0, 1 - cos 0.6]: 2x g(x) with g a
+// cubic least-squares fit (on Chebyshev nodes of that interval) of
+// g(x) = (2 asin(sqrt(x / 2)))^2 / (2x), relative error < 2e-7.  The
+// interpolation weights below depend on th^2 only weakly (their derivative
+// in th^2 is below 0.1), so neither this error nor the rounding of
+// 1 - cos(th) near th = 0 moves them by more than ~1e-8.
+__device__ __forceinline__ float acos_sq(float x) {
+   float g = 0.01572742f;
+   g = fmaf(g, x, 0.0443475f);
+   g = fmaf(g, x, 0.16666762f);
+   g = fmaf(g, x, 1.f);
+   return (x + x) * g;
+}
+
 // SphericalInterpolation (simulator.cpp:473-494) in FP32.  The weights
 // sin((1-t)th)/sin(th) and sin(t th)/sin(th) are evaluated as
 // (1-t) S((1-t)^2 th^2) / S(th^2) and t S(t^2 th^2) / S(th^2), S(y) =
-// sin(sqrt y)/sqrt y, for th < 0.6 (smooth fibre fields), which needs no
-// sine calls and stays accurate as th -> 0; larger angles use sinf.
+// sin(sqrt y)/sqrt y, for th < 0.6 (smooth fibre fields), with th^2 taken
+// from cos(th) directly (acos_sq): no inverse cosine and no sine calls, and
+// accurate as th -> 0.  Larger angles use acosf and the hardware sine.  The
+// reference's flip of u (when v.u < 0) is carried as the sign of u's weight.
 __device__ __forceinline__ F3 slerp_axis(F3 v, F3 u, float t) {
    if (is_zero(v))
       return u;
    if (is_zero(u))
       return v;
-   float d = dot3(v, u);
-   if (d < 0.f) {
-      u = F3{-u.x, -u.y, -u.z};
-      d = -d;
-   }
-   const F3 df{v.x - u.x, v.y - u.y, v.z - u.z};
+   const float d0 = dot3(v, u);
+   const float sg = d0 < 0.f ? -1.f : 1.f;
+   const F3 df{fmaf(-sg, u.x, v.x), fmaf(-sg, u.y, v.y), fmaf(-sg, u.z, v.z)};
    if (dot3(df, df) < 1e-12f)
       return v;
-   const float c = fminf(d * rsqrtf(dot3(v, v) * dot3(u, u)), 1.f);
-   const float th = acosf(c);
+   const float c = fminf(fabsf(d0) * rsqrtf(dot3(v, v) * dot3(u, u)), 1.f);
    float w0, w1;
-   if (th < 0.6f) {
-      const float y = th * th, s = 1.f - t;
+   if (c > 0.825335615f) { // th < 0.6
+      const float y = acos_sq(1.f - c), s = 1.f - t;
       const float inv = __fdividef(1.f, sinc_sq(y));
       w0 = s * sinc_sq(s * s * y) * inv;
       w1 = t * sinc_sq(t * t * y) * inv;
    } else { // th in [0.6, pi/2]: the hardware sine is accurate to ~5e-7 here
+      const float th = acosf(c);
       const float inv = __fdividef(1.f, __sinf(th));
       w0 = __sinf((1.f - t) * th) * inv;
       w1 = __sinf(t * th) * inv;
    }
+   w1 *= sg;
    return F3{fmaf(v.x, w0, u.x * w1), fmaf(v.y, w0, u.y * w1), fmaf(v.z, w0, u.z * w1)};
 }
 
