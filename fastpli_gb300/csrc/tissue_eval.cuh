@@ -44,23 +44,25 @@ FPGB_HD void closest_point(const SegDev &S, const double pt[3],
 // bound: the float that
 // the reference's double arithmetic produces (exact_dist) lies in
 // [d2f - margin, d2f + margin].  The bound covers the rounding of the float
-// inputs, of every FP32 operation, of the branch decision (the distance is
-// continuous across the branches) and of the reference's own final rounding;
-// a host build checks it over every voxel of random segment boxes.
+// inputs, of every FP32 operation (written as fused multiply-adds: one
+// rounding each, the same on the host and the device), of the branch
+// decision (the distance is continuous across the branches) and of the
+// reference's own final rounding; a host build checks it over every voxel of
+// random segment boxes.
 FPGB_HD float approx_dist2(float wx, float wy, float wz, float vx, float vy, float vz,
                            float c2f, float rc2, float &margin) {
-   const float c1f = wx * vx + wy * vy + wz * vz;
-   const float w2 = wx * wx + wy * wy + wz * wz;
+   const float c1f = fmaf(wz, vz, fmaf(wy, vy, wx * vx));
+   const float w2 = fmaf(wz, wz, fmaf(wy, wy, wx * wx));
    float d2f;
    if (c1f <= 0.f) {
       d2f = w2;
    } else if (c1f >= c2f) {
       const float ux = wx - vx, uy = wy - vy, uz = wz - vz;
-      d2f = ux * ux + uy * uy + uz * uz;
+      d2f = fmaf(uz, uz, fmaf(uy, uy, ux * ux));
    } else {
-      d2f = w2 - c1f * (c1f * rc2);
+      d2f = fmaf(-c1f, c1f * rc2, w2);
    }
-   margin = 1e-4f + 3.8e-6f * (w2 + c2f);
+   margin = fmaf(3.8e-6f, w2 + c2f, 1e-4f);
    return d2f;
 }
 

@@ -188,14 +188,71 @@ __device__ __forceinline__ SegFP32 seg_fp32(const SegDev &S) {
                   S.c2_rcp, S.thr_f, S.acc_f, S.base[0], S.base[1], S.base[2]};
 }
 
-// FP32 estimate of the candidate (segment, voxel x y z): its dist^2 lies in
-// [lo, hi] (directed rounding of estimate -/+ bound).
-__device__ __forceinline__ void candidate_bounds(const SegFP32 &g, int x, int y, int z, float &lo,
-                                                 float &hi) {
+// Lane-dense walk over a sub-box: lane l visits the voxels k = l, l + 32,
+// l + 64, ... of the flattened (x, y, z) order.  The position advances by 32
+// with mixed-radix carries (z into y, y into x; one carry each at most, since
+// the step's z and y parts are below ez and ey), and the brick index and the
+// float offsets (x - base) + 1/2 — half-integers, exact in float — advance
+// with it, so the sweep does no division or int/float conversion per voxel.
+struct BoxWalk {
+   int k, n, li, dli, cz, cy;
+   float gx, gy, gz, dgx, dgy, dgz, gz_end, gy_end, fez, fey;
+};
+
+__device__ __forceinline__ BoxWalk box_walk(const SubBox &b, const SegFP32 &g, int ox, int oy,
+                                            int oz, int lane) {
+   BoxWalk w;
+   int x, y, z, sx, sy, sz;
+   sub_box_voxel(b, lane, x, y, z);
+   sub_box_voxel(b, 32, sx, sy, sz); // voxel 32 relative to voxel 0: the step
+   sx -= b.x0;
+   sy -= b.y0;
+   sz -= b.z0;
+   w.k = lane;
+   w.n = b.n;
+   w.li = brick_index(x, y, z, ox, oy, oz);
+   w.dli = (sx * kBrickY + sy) * kBrickZ + sz;
+   w.cz = kBrickZ - b.ez;             // z carry: z -= ez, y += 1
+   w.cy = (kBrickY - b.ey) * kBrickZ; // y carry: y -= ey, x += 1
+   w.gx = (float)(x - g.bx) + 0.5f;
+   w.gy = (float)(y - g.by) + 0.5f;
+   w.gz = (float)(z - g.bz) + 0.5f;
+   w.dgx = (float)sx;
+   w.dgy = (float)sy;
+   w.dgz = (float)sz;
+   w.gz_end = (float)(b.z0 + b.ez - g.bz) + 0.5f;
+   w.gy_end = (float)(b.y0 + b.ey - g.by) + 0.5f;
+   w.fez = (float)b.ez;
+   w.fey = (float)b.ey;
+   return w;
+}
+
+__device__ __forceinline__ void box_step(BoxWalk &w) {
+   w.k += 32;
+   w.li += w.dli;
+   w.gx += w.dgx;
+   w.gy += w.dgy;
+   w.gz += w.dgz;
+   if (w.gz >= w.gz_end) {
+      w.gz -= w.fez;
+      w.gy += 1.f;
+      w.li += w.cz;
+   }
+   if (w.gy >= w.gy_end) {
+      w.gy -= w.fey;
+      w.gx += 1.f;
+      w.li += w.cy;
+   }
+}
+
+// FP32 estimate of the candidate (segment, voxel at offsets g* from the
+// segment's base): its dist^2 lies in [lo, hi] (directed rounding of
+// estimate -/+ bound).
+__device__ __forceinline__ void candidate_bounds(const SegFP32 &g, float gx, float gy, float gz,
+                                                 float &lo, float &hi) {
    float mg;
-   const float d2f = approx_dist2((float)(x - g.bx) + 0.5f - g.pfx, (float)(y - g.by) + 0.5f - g.pfy,
-                                  (float)(z - g.bz) + 0.5f - g.pfz, g.vx, g.vy, g.vz, g.c2f, g.rc2,
-                                  mg);
+   const float d2f = approx_dist2(gx - g.pfx, gy - g.pfy, gz - g.pfz, g.vx, g.vy, g.vz, g.c2f,
+                                  g.rc2, mg);
    lo = __fsub_rd(d2f, mg);
    hi = __fadd_ru(d2f, mg);
 }
@@ -207,17 +264,14 @@ __device__ __forceinline__ void brick_bound(const SegDev &S, const SubBox &b, in
                                             int lane) {
    const SegFP32 g = seg_fp32(S);
    const unsigned bundle = (unsigned)S.bundle;
-   for (int k = lane; k < b.n; k += 32) {
-      int x, y, z;
-      sub_box_voxel(b, k, x, y, z);
+   for (BoxWalk w = box_walk(b, g, ox, oy, oz, lane); w.k < w.n; box_step(w)) {
       float lo, hi;
-      candidate_bounds(g, x, y, z, lo, hi);
+      candidate_bounds(g, w.gx, w.gy, w.gz, lo, hi);
       if (!(hi <= g.acc))
          continue;
-      const int li = brick_index(x, y, z, ox, oy, oz);
-      atomicMin(&skey[li], ((unsigned long long)__float_as_uint(hi) << 32) | 0xFFFFFFFFull);
+      atomicMin(&skey[w.li], ((unsigned long long)__float_as_uint(hi) << 32) | 0xFFFFFFFFull);
       if (MULTI)
-         atomicMin(&sminb[li], bundle);
+         atomicMin(&sminb[w.li], bundle);
    }
 }
 
@@ -278,18 +332,16 @@ __device__ __forceinline__ void brick_filter(const SegDev &S, unsigned slot, con
                                              const LayerDev *__restrict__ layers, int layer_base,
                                              unsigned *sminb, unsigned long long &n_slow) {
    const SegFP32 g = seg_fp32(S);
-   for (int k0 = 0; k0 < b.n; k0 += 32) {
-      const int k = k0 + lane;
+   BoxWalk w = box_walk(b, g, ox, oy, oz, lane);
+   for (int k0 = 0; k0 < b.n; k0 += 32, box_step(w)) {
       bool need = false;
       unsigned short e = 0;
-      if (k < b.n) {
-         int x, y, z;
-         sub_box_voxel(b, k, x, y, z);
+      if (w.k < w.n) {
          float lo, hi;
-         candidate_bounds(g, x, y, z, lo, hi);
+         candidate_bounds(g, w.gx, w.gy, w.gz, lo, hi);
          if (!(lo > g.thr)) { // inside the outermost layer at the thickest end
             const bool certain = hi <= g.acc;
-            const int li = brick_index(x, y, z, ox, oy, oz);
+            const int li = w.li;
             // keys only decrease, so any value read bounds the final one from
             // above; the initial ~0 reads as NaN and skips nothing
             const unsigned long long cur =

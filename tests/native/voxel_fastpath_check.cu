@@ -6,6 +6,8 @@
 //
 //   nvcc -O2 -std=c++17 -fmad=false -Xcompiler -ffp-contract=off \
 //        -I include tests/native/voxel_fastpath_check.cu -o check && ./check SEED N
+#include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <random>
@@ -62,6 +64,7 @@ int main(int argc, char **argv) {
    }
    long long n = 0, fast = 0, bad = 0, vec_fast = 0, vec_bad = 0;
    long long bound_bad = 0, certain = 0, certain_bad = 0;
+   double worst = 0.0; // largest |reference - estimate| / bound
    for (const SegDev &S : plan.segs) {
       for (int ix = 0; ix < S.ext[0]; ix++)
          for (int iy = 0; iy < S.ext[1]; iy++)
@@ -80,6 +83,7 @@ int main(int argc, char **argv) {
                const float d2f = approx_dist2(lpt[0] - S.pf[0], lpt[1] - S.pf[1],
                                               lpt[2] - S.pf[2], S.vf[0], S.vf[1], S.vf[2],
                                               S.c2f, S.c2_rcp, mg);
+               worst = std::max(worst, std::fabs((double)d_ex - (double)d2f) / (double)mg);
                if (!((double)d_ex <= (double)d2f + mg && (double)d_ex >= (double)d2f - mg)) {
                   if (bound_bad < 5)
                      printf("BOUND dist %.9g estimate %.9g margin %.3g\n", d_ex, d2f, mg);
@@ -117,8 +121,9 @@ int main(int argc, char **argv) {
             }
    }
    printf("candidates %lld fast %lld (%.6f) mismatches %lld vectors_fast %lld vector_mismatches %lld"
-          " bound_violations %lld certain %lld certain_rejected %lld\n",
-          n, fast, n ? (double)fast / n : 0.0, bad, vec_fast, vec_bad, bound_bad, certain,
+          " bound_violations %lld (largest error %.3f of the bound) certain %lld"
+          " certain_rejected %lld\n",
+          n, fast, n ? (double)fast / n : 0.0, bad, vec_fast, vec_bad, bound_bad, worst, certain,
           certain_bad);
    return (bad || vec_bad || bound_bad || certain_bad) ? 1 : 0;
 }
