@@ -275,6 +275,59 @@ __device__ __forceinline__ void brick_bound(const SegDev &S, const SubBox &b, in
    }
 }
 
+// Exact evaluation of one candidate: the two-float path, with the FP64
+// replay of the reference arithmetic for the few it leaves undecided.  Out of
+// line: one shared copy of these large bodies keeps the sweep loops that call
+// them small in the instruction cache.
+//
+// float(|closest - point|^2) and float(r(t)^2) (generator.cpp:327-328) of
+// (S, voxel x y z); returns true when the FP64 replay ran.
+__device__ __noinline__ bool cand_dist(const SegDev &S, int x, int y, int z, float &dist_squ,
+                                       float &r_sqr) {
+   const float lpt[3] = {(float)(x - S.base[0]) + 0.5f, (float)(y - S.base[1]) + 0.5f,
+                         (float)(z - S.base[2]) + 0.5f};
+   FastCand fc;
+   if (S.pscale < 0x1p22f && fast_candidate(S, lpt, fc)) {
+      dist_squ = fc.dist_squ;
+      r_sqr = fc.r_sqr;
+      return false;
+   }
+   const double pt[3] = {(double)x + 0.5, (double)y + 0.5, (double)z + 0.5};
+   double cl[3];
+   exact_dist(S, pt, cl, dist_squ, r_sqr);
+   return true;
+}
+
+// float(vm::unit(point - closest)) of the 'r' layer (generator.cpp:365-371);
+// returns true when the FP64 replay ran.
+__device__ __noinline__ bool cand_radial(const SegDev &S, int x, int y, int z, float o[3]) {
+   const float lpt[3] = {(float)(x - S.base[0]) + 0.5f, (float)(y - S.base[1]) + 0.5f,
+                         (float)(z - S.base[2]) + 0.5f};
+   FastCand fc;
+   if (S.pscale < 0x1p22f && fast_candidate(S, lpt, fc) && fast_radial(S, fc, o))
+      return false;
+   const double pt[3] = {(double)x + 0.5, (double)y + 0.5, (double)z + 0.5};
+   double cl[3];
+   float d_chk, r_chk;
+   exact_dist(S, pt, cl, d_chk, r_chk);
+   // unit vector in the reference's double order
+   double nv[3] = {pt[0] - cl[0], pt[1] - cl[1], pt[2] - cl[2]};
+   double n2 = 0.0;
+   n2 = n2 + nv[0] * nv[0];
+   n2 = n2 + nv[1] * nv[1];
+   n2 = n2 + nv[2] * nv[2];
+   if (n2 > 0) {
+      const double inv = 1.0 / sqrt(n2);
+      nv[0] = nv[0] * inv;
+      nv[1] = nv[1] * inv;
+      nv[2] = nv[2] * inv;
+   }
+   o[0] = (float)nv[0];
+   o[1] = (float)nv[1];
+   o[2] = (float)nv[2];
+   return true;
+}
+
 // Queue entry flags (bits 0-10: voxel of the brick)
 constexpr unsigned short kQueueCertain = 1u << 14;    // certainly accepted
 constexpr unsigned short kQueueBundleOnly = 1u << 15; // cannot win; bundle minimum only
@@ -299,18 +352,8 @@ __device__ __forceinline__ void brick_eval(const SegDev *__restrict__ segs,
    const int li = e & (kBrickVoxels - 1);
    const int x = ox + (li >> 8), y = oy + ((li >> 5) & 7), z = oz + (li & 31);
    float dist_squ, r_sqr;
-   FastCand fc;
-   const float lpt[3] = {(float)(x - S.base[0]) + 0.5f, (float)(y - S.base[1]) + 0.5f,
-                         (float)(z - S.base[2]) + 0.5f};
-   if (S.pscale < 0x1p22f && fast_candidate(S, lpt, fc)) {
-      dist_squ = fc.dist_squ;
-      r_sqr = fc.r_sqr;
-   } else {
-      const double pt[3] = {(double)x + 0.5, (double)y + 0.5, (double)z + 0.5};
-      double cl[3];
-      exact_dist(S, pt, cl, dist_squ, r_sqr);
+   if (cand_dist(S, x, y, z, dist_squ, r_sqr))
       n_slow++;
-   }
    if (dist_squ > layers[layer_base + S.bundle].f_ly_squ * r_sqr) // generator.cpp:329-331
       return;
    if (!(e & kQueueBundleOnly))
@@ -395,27 +438,14 @@ __device__ __forceinline__ void decode_voxel(unsigned long long key, int x, int 
    const LayerDev &L = layers[layer_base + S.bundle];
    // With a constant radius whose square rounds the same at every t
    // (rsq_const) and at both ends, r^2 at the winner is known without
-   // evaluating the candidate again; only the radial model then needs it.
+   // evaluating the candidate again.
    const bool r_known = S.rsq_const == S.rsq0 && S.rsq_const == S.rsq1; // false for NaN
-   FastCand fc;
-   bool fast = false, evaluated = false;
    float r_sqr = S.rsq_const;
-   double cl[3];
-   auto evaluate = [&]() {
-      const float lpt[3] = {(float)(x - S.base[0]) + 0.5f, (float)(y - S.base[1]) + 0.5f,
-                            (float)(z - S.base[2]) + 0.5f};
-      fast = S.pscale < 0x1p22f && fast_candidate(S, lpt, fc);
-      float r2 = fc.r_sqr;
-      if (!fast) {
-         const double pt[3] = {(double)x + 0.5, (double)y + 0.5, (double)z + 0.5};
-         float d_chk;
-         exact_dist(S, pt, cl, d_chk, r2);
-      }
-      evaluated = true;
-      return r2;
-   };
-   if (!r_known)
-      r_sqr = evaluate();
+   if (!r_known) {
+      float d_chk;
+      if (cand_dist(S, x, y, z, d_chk, r_sqr))
+         n_slow++;
+   }
    // std::lower_bound(scale^2, double(dist_squ / r_sqr)) (generator.cpp:345-349)
    const float qv = dist_squ / r_sqr;
    int ly = 0;
@@ -433,34 +463,8 @@ __device__ __forceinline__ void decode_voxel(unsigned long long key, int x, int 
       o[0] = S.vp[0];
       o[1] = S.vp[1];
       o[2] = S.vp[2];
-   } else if (m == 'r') {
-      if (!evaluated) { // the caller evaluates it with radial_vector, 32 at a time
-         defer = true;
-         return;
-      }
-      if (!(fast && fast_radial(S, fc, o))) {
-         const double pt[3] = {(double)x + 0.5, (double)y + 0.5, (double)z + 0.5};
-         if (fast) {
-            float d_chk, r_chk;
-            exact_dist(S, pt, cl, d_chk, r_chk);
-         }
-         n_slow++;
-         // vm::unit(point - closest) in the reference's double order
-         double nv[3] = {pt[0] - cl[0], pt[1] - cl[1], pt[2] - cl[2]};
-         double n2 = 0.0;
-         n2 = n2 + nv[0] * nv[0];
-         n2 = n2 + nv[1] * nv[1];
-         n2 = n2 + nv[2] * nv[2];
-         if (n2 > 0) {
-            const double inv = 1.0 / sqrt(n2);
-            nv[0] = nv[0] * inv;
-            nv[1] = nv[1] * inv;
-            nv[2] = nv[2] * inv;
-         }
-         o[0] = (float)nv[0];
-         o[1] = (float)nv[1];
-         o[2] = (float)nv[2];
-      }
+   } else if (m == 'r') { // the caller evaluates it with radial_vector, 32 at a time
+      defer = true;
    }
 }
 
@@ -468,31 +472,8 @@ __device__ __forceinline__ void decode_voxel(unsigned long long key, int x, int 
 // (generator.cpp:365-371) by the two-float path, FP64 replay when undecided.
 __device__ __forceinline__ void radial_vector(const SegDev &S, int x, int y, int z, float o[3],
                                               unsigned long long &n_slow) {
-   const float lpt[3] = {(float)(x - S.base[0]) + 0.5f, (float)(y - S.base[1]) + 0.5f,
-                         (float)(z - S.base[2]) + 0.5f};
-   FastCand fc;
-   const bool fast = S.pscale < 0x1p22f && fast_candidate(S, lpt, fc);
-   if (fast && fast_radial(S, fc, o))
-      return;
-   const double pt[3] = {(double)x + 0.5, (double)y + 0.5, (double)z + 0.5};
-   double cl[3];
-   float d_chk, r_chk;
-   exact_dist(S, pt, cl, d_chk, r_chk);
-   n_slow++;
-   double nv[3] = {pt[0] - cl[0], pt[1] - cl[1], pt[2] - cl[2]};
-   double n2 = 0.0;
-   n2 = n2 + nv[0] * nv[0];
-   n2 = n2 + nv[1] * nv[1];
-   n2 = n2 + nv[2] * nv[2];
-   if (n2 > 0) {
-      const double inv = 1.0 / sqrt(n2);
-      nv[0] = nv[0] * inv;
-      nv[1] = nv[1] * inv;
-      nv[2] = nv[2] * inv;
-   }
-   o[0] = (float)nv[0];
-   o[1] = (float)nv[1];
-   o[2] = (float)nv[2];
+   if (cand_radial(S, x, y, z, o))
+      n_slow++;
 }
 
 // ------------------------------------------------------------- the brick ---
