@@ -417,8 +417,10 @@ __device__ __forceinline__ void apply_retard(float &u1, float &u2, float &u3, fl
    u2 = fmaf(-a1, s, b1 * c);
 }
 
-// One CCD-pixel ray, one thread, every step in order.  Used for NN, where a
-// birefringent step costs one vector load.
+// One CCD-pixel ray, one thread, every step in order.  The label of step
+// k + 1 is loaded while step k is worked on, and a step's kind comes from a
+// register mask (labels below 16), so the cheap steps wait on one load
+// instead of a chain of two.
 template <int MODE, bool TILT, bool WIDE>
 __device__ __forceinline__ void march_one_ray(const MarchParams &P, int64_t ray,
                                               const int32_t *__restrict__ label,
@@ -431,6 +433,7 @@ __device__ __forceinline__ void march_one_ray(const MarchParams &P, int64_t ray,
    using C = typename MarchIdx<WIDE>::C;
    using U = typename MarchIdx<WIDE>::U;
    const int F = P.frac_bits;
+   const int n_z = P.n_z;
    int64_t px, py;
    ray_setup(P, ray, px, py);
    float u1 = 0.f, u2 = 0.f, u3 = -1.f, L = 0.f;
@@ -438,53 +441,68 @@ __device__ __forceinline__ void march_one_ray(const MarchParams &P, int64_t ray,
    const C X = (C)P.X, Y = (C)P.Y;
    C ix = fx_floor<WIDE>(px, F), iy = fx_floor<WIDE>(py, F);
    bool inside = ix >= 0 && ix < X && iy >= 0 && iy < Y;
-   for (int k = 0; k < P.n_z; k++) {
-      if (TILT && k > 0) {
-         px += P.dx_fx;
-         py += P.dy_fx;
-         ix = fx_floor<WIDE>(px, F);
-         iy = fx_floor<WIDE>(py, F);
+   U idx = 0;
+   int lab = 0;
+   if (inside && n_z > 0) {
+      idx = voxel_index<WIDE>(P, ix, iy, (C)P.ztab[0].iz);
+      lab = __ldg(label + idx);
+   }
+   for (int k = 0; k < n_z; k++) {
+      // next step's position and label
+      if (TILT) {
+         ix = fx_floor<WIDE>(px + P.dx_fx, F);
+         iy = fx_floor<WIDE>(py + P.dy_fx, F);
          inside = ix >= 0 && ix < X && iy >= 0 && iy < Y;
       }
-      const ZStep zs = P.ztab[k];
-      int lab = 0;
-      U idx = 0;
-      if (inside) {
-         idx = voxel_index<WIDE>(P, ix, iy, (C)zs.iz);
-         lab = __ldg(label + idx);
-         if (lab < 0 || lab >= P.n_props) {
+      U idx_n = 0;
+      int lab_n = 0;
+      if (inside && k + 1 < n_z) {
+         idx_n = voxel_index<WIDE>(P, ix, iy, (C)P.ztab[k + 1].iz);
+         lab_n = __ldg(label + idx_n);
+      }
+      // step k
+      [&] {
+         if (lab < 0 || lab >= P.n_props) { // (0 outside the volume)
             bad_label = true;
             lab = 0;
          }
-      }
-      const LabelOptics o = P.lut[lab];
-      if (o.kind == 0)
-         continue;
-      if (o.kind == 1) {
+         const int kind = P.kind_packed ? (int)((P.kind_mask >> (2 * lab)) & 3u)
+                                        : P.lut[lab].kind;
+         if (kind == 0)
+            return;
+         const LabelOptics o = P.lut[lab];
+         if (kind == 1) {
+            L += o.alog;
+            return;
+         }
+         F3 v;
+         if (MODE == 0)
+            v = load_vec(vec, idx);
+         else
+            v = axis_interp<MODE, WIDE>(P, label, vec, px, py, P.ztab[k], lab);
+         if (is_zero(v)) { // simulator.cpp:292-297: no attenuation either
+            w_zero = true;
+            return;
+         }
+         const float n2 = dot3(v, v);
+         if (n2 - 1.f > 1e-5f)
+            w_norm = true;
+         if (TILT && P.rotate) {
+            v = F3{dot3(F3{P.rot[0], P.rot[1], P.rot[2]}, v),
+                   dot3(F3{P.rot[3], P.rot[4], P.rot[5]}, v),
+                   dot3(F3{P.rot[6], P.rot[7], P.rot[8]}, v)};
+         }
+         float c, s, cr, sr;
+         if (retard_params(v, n2, o.kret, c, s, cr, sr))
+            apply_retard(u1, u2, u3, c, s, cr, sr);
          L += o.alog;
-         continue;
+      }();
+      if (TILT) {
+         px += P.dx_fx;
+         py += P.dy_fx;
       }
-      F3 v;
-      if (MODE == 0)
-         v = load_vec(vec, idx);
-      else
-         v = axis_interp<MODE, WIDE>(P, label, vec, px, py, zs, lab);
-      if (is_zero(v)) { // simulator.cpp:292-297: no attenuation either
-         w_zero = true;
-         continue;
-      }
-      const float n2 = dot3(v, v);
-      if (n2 - 1.f > 1e-5f)
-         w_norm = true;
-      if (TILT && P.rotate) {
-         v = F3{dot3(F3{P.rot[0], P.rot[1], P.rot[2]}, v),
-                dot3(F3{P.rot[3], P.rot[4], P.rot[5]}, v),
-                dot3(F3{P.rot[6], P.rot[7], P.rot[8]}, v)};
-      }
-      float c, s, cr, sr;
-      if (retard_params(v, n2, o.kret, c, s, cr, sr))
-         apply_retard(u1, u2, u3, c, s, cr, sr);
-      L += o.alog;
+      idx = idx_n;
+      lab = lab_n;
    }
    ray_epilogue(P, ray, u1, u2, L, image, epa_t, epa_d, epa_r, w_zero, w_norm, bad_label,
                 counters);

@@ -195,6 +195,10 @@ int plan_march(const fpgb_setup *s, const int64_t *dim, const double *props, int
          o.kind = 2;
       o.pad = 0;
    }
+   P.kind_packed = n_props <= 16 ? 1 : 0;
+   P.kind_mask = 0;
+   for (int64_t l = 0; l < n_props && l < 16; l++)
+      P.kind_mask |= (uint32_t)plan->lut[l].kind << (2 * l);
 
    // tilt (simulator.cpp:216-231, 585-590)
    double rot[9];

@@ -58,7 +58,11 @@ struct MarchParams {
    // march (steps needing interpolation compacted across the warp), 0 = one
    // thread per ray.  Both give the same bits; the choice is speed only.
    int32_t coop;
-   int32_t pad_[3];
+   // kinds of labels 0..15, two bits each (kind_packed = 1 when every label
+   // fits): the march reads a step's kind without a table load
+   uint32_t kind_mask;
+   int32_t kind_packed;
+   int32_t pad_;
 };
 static_assert(sizeof(MarchParams) % 16 == 0, "MarchParams is staged in 16-byte words");
 
