@@ -1,6 +1,7 @@
 // Voxelizer data layout shared by the plain, batched and no-allocation paths.
 #pragma once
 
+#include <cstddef>
 #include <cstdint>
 #include <memory>
 #include <vector>
@@ -13,15 +14,18 @@ constexpr int kMaxLayers = 16;
 
 // One fiber segment after translate + resize (voxel units), in the
 // reference's processing order; its table index is the tie-break index.
-struct SegDev {
+struct __align__(16) SegDev {
    double p[3];   // segment start s0
    double q[3];   // segment end s1
    double v[3];   // s1 - s0 (generator.cpp:479)
    double r0, r1; // radii at s0, s1
    double c2;     // dot(v, v) (generator.cpp:486)
+   // inputs of the voxelizer's sweeps: five 16-byte words at offset 96,
+   // read with vector loads (SegSweep)
    float pf[3];   // p - base, for the FP32 prefilter
    float vf[3];   // float(v)
    float c2f;     // float(c2)
+   float c2_rcp;  // float(1 / c2)
    float thr_f;   // prefilter bound on dist^2 (>= f_ly_squ * max(r0,r1)^2)
    float acc_f;   // dist^2 at or below which a candidate is certainly inside
                   // (<= f_ly_squ * min(r0,r1)^2, rounded down)
@@ -33,7 +37,6 @@ struct SegDev {
    float pl_hi[3], pl_lo[3]; // p - base
    float v_hi[3], v_lo[3];   // v
    float c2_hi, c2_lo;       // c2
-   float c2_rcp;             // float(1 / c2)
    float r0_hi, r0_lo;       // r0
    float dr_hi, dr_lo;       // r1 - r0
    float rsq0, rsq1;         // float(r^2) at t = 0 and t = 1 (exact)
@@ -42,6 +45,8 @@ struct SegDev {
    float pscale;             // max |coordinate| met by this segment's arithmetic
    float vp[3];              // float(unit(q - p)): the 'p' layer vector (exact)
 };
+static_assert(offsetof(SegDev, pf) == 96 && offsetof(SegDev, bundle) == 172,
+              "the sweep inputs of SegDev are five aligned 16-byte words");
 
 // Layers of one bundle, sorted by scale (fiber_bundle.cpp:83-86).
 struct LayerDev {

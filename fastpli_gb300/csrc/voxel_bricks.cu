@@ -138,6 +138,22 @@ brick_scan(const unsigned *__restrict__ counts, int64_t n, unsigned *__restrict_
 }
 
 // ------------------------------------------------------------ key passes ---
+// The inputs of the sweeps of one segment (SegDev offsets 96..175: pf, vf,
+// c2f, c2_rcp, thr_f, acc_f, base, lo, ext, bundle) in five 16-byte loads.
+struct SegSweep {
+   float4 a; // pf[0..2], vf[0]
+   float4 b; // vf[1..2], c2f, c2_rcp
+   float4 c; // thr_f, acc_f, base[0..1] (int bits)
+   int4 d;   // base[2], lo[0..2]
+   int4 e;   // ext[0..2], bundle
+};
+
+__device__ __forceinline__ SegSweep load_sweep(const SegDev &S) {
+   const float4 *f = reinterpret_cast<const float4 *>(&S.pf[0]);
+   const int4 *i = reinterpret_cast<const int4 *>(&S.pf[0]);
+   return SegSweep{__ldg(f), __ldg(f + 1), __ldg(f + 2), __ldg(i + 3), __ldg(i + 4)};
+}
+
 // The part of segment S's clipped box inside the brick (origin o, extent n),
 // walked by a warp 32 voxels at a time in a flattened (x, y, z) order.
 struct SubBox {
@@ -145,19 +161,19 @@ struct SubBox {
    float inv_ez, inv_eyz; // 1/ez, 1/(ey*ez) for division-free index splits
 };
 
-__device__ __forceinline__ bool sub_box(const SegDev &S, int ox, int oy, int oz, int nx, int ny,
-                                        int nz, SubBox &b) {
-   b.x0 = max(S.lo[0], ox);
-   b.y0 = max(S.lo[1], oy);
-   b.z0 = max(S.lo[2], oz);
-   const int ex = min(S.lo[0] + S.ext[0], ox + nx) - b.x0;
-   b.ey = min(S.lo[1] + S.ext[1], oy + ny) - b.y0;
-   b.ez = min(S.lo[2] + S.ext[2], oz + nz) - b.z0;
+__device__ __forceinline__ bool sub_box(const SegSweep &w, int ox, int oy, int oz, int nx,
+                                        int ny, int nz, SubBox &b) {
+   b.x0 = max(w.d.y, ox);
+   b.y0 = max(w.d.z, oy);
+   b.z0 = max(w.d.w, oz);
+   const int ex = min(w.d.y + w.e.x, ox + nx) - b.x0;
+   b.ey = min(w.d.z + w.e.y, oy + ny) - b.y0;
+   b.ez = min(w.d.w + w.e.z, oz + nz) - b.z0;
    if (ex <= 0 || b.ey <= 0 || b.ez <= 0)
       return false;
    b.n = ex * b.ey * b.ez;
-   b.inv_ez = 1.f / (float)b.ez;
-   b.inv_eyz = 1.f / (float)(b.ey * b.ez);
+   b.inv_ez = __frcp_rn((float)b.ez);
+   b.inv_eyz = __frcp_rn((float)(b.ey * b.ez));
    return true;
 }
 
@@ -183,9 +199,9 @@ struct SegFP32 {
    int bx, by, bz;
 };
 
-__device__ __forceinline__ SegFP32 seg_fp32(const SegDev &S) {
-   return SegFP32{S.pf[0], S.pf[1], S.pf[2], S.vf[0], S.vf[1], S.vf[2], S.c2f,
-                  S.c2_rcp, S.thr_f, S.acc_f, S.base[0], S.base[1], S.base[2]};
+__device__ __forceinline__ SegFP32 seg_fp32(const SegSweep &w) {
+   return SegFP32{w.a.x, w.a.y, w.a.z, w.a.w, w.b.x, w.b.y, w.b.z, w.b.w, w.c.x, w.c.y,
+                  __float_as_int(w.c.z), __float_as_int(w.c.w), w.d.x};
 }
 
 // Lane-dense walk over a sub-box: lane l visits the voxels k = l, l + 32,
@@ -259,11 +275,11 @@ __device__ __forceinline__ void candidate_bounds(const SegFP32 &g, float gx, flo
 
 // BOUND pass of one segment over its sub-box.
 template <bool MULTI>
-__device__ __forceinline__ void brick_bound(const SegDev &S, const SubBox &b, int ox, int oy,
+__device__ __forceinline__ void brick_bound(const SegSweep &sw, const SubBox &b, int ox, int oy,
                                             int oz, unsigned long long *skey, unsigned *sminb,
                                             int lane) {
-   const SegFP32 g = seg_fp32(S);
-   const unsigned bundle = (unsigned)S.bundle;
+   const SegFP32 g = seg_fp32(sw);
+   const unsigned bundle = (unsigned)sw.e.w;
    for (BoxWalk w = box_walk(b, g, ox, oy, oz, lane); w.k < w.n; box_step(w)) {
       float lo, hi;
       candidate_bounds(g, w.gx, w.gy, w.gz, lo, hi);
@@ -367,14 +383,14 @@ __device__ __forceinline__ void brick_eval(const SegDev *__restrict__ segs,
 // still win (or, for the bundle minimum, might be accepted) go to the warp's
 // queue, which is drained 32 entries at a time by all lanes together.
 template <bool MULTI>
-__device__ __forceinline__ void brick_filter(const SegDev &S, unsigned slot, const SubBox &b,
+__device__ __forceinline__ void brick_filter(const SegSweep &sw, unsigned slot, const SubBox &b,
                                              int ox, int oy, int oz, unsigned long long *skey,
                                              WarpQueue &q, int &qn, int lane,
                                              const SegDev *__restrict__ segs,
                                              const unsigned *__restrict__ list,
                                              const LayerDev *__restrict__ layers, int layer_base,
                                              unsigned *sminb, unsigned long long &n_slow) {
-   const SegFP32 g = seg_fp32(S);
+   const SegFP32 g = seg_fp32(sw);
    BoxWalk w = box_walk(b, g, ox, oy, oz, lane);
    for (int k0 = 0; k0 < b.n; k0 += 32, box_step(w)) {
       bool need = false;
@@ -532,10 +548,10 @@ voxel_bricks(const SegDev *__restrict__ segs, const TileDev *__restrict__ tiles,
          j = __shfl_sync(0xFFFFFFFFu, j, 0) + j0;
          if (j >= j1)
             break;
-         const SegDev &S = segs[list[j]];
+         const SegSweep sw = load_sweep(segs[list[j]]);
          SubBox b;
-         if (sub_box(S, ox, oy, oz, nx, ny, nz, b))
-            brick_bound<MULTI>(S, b, ox, oy, oz, skey, sminb, lane);
+         if (sub_box(sw, ox, oy, oz, nx, ny, nz, b))
+            brick_bound<MULTI>(sw, b, ox, oy, oz, skey, sminb, lane);
       }
       __syncthreads();
       // EXACT pass
@@ -549,10 +565,10 @@ voxel_bricks(const SegDev *__restrict__ segs, const TileDev *__restrict__ tiles,
             j = __shfl_sync(0xFFFFFFFFu, j, 0) + j0;
             if (j >= j1)
                break;
-            const SegDev &S = segs[list[j]];
+            const SegSweep sw = load_sweep(segs[list[j]]);
             SubBox b;
-            if (sub_box(S, ox, oy, oz, nx, ny, nz, b))
-               brick_filter<MULTI>(S, j, b, ox, oy, oz, skey, q, qn, lane, segs, list, layers,
+            if (sub_box(sw, ox, oy, oz, nx, ny, nz, b))
+               brick_filter<MULTI>(sw, j, b, ox, oy, oz, skey, q, qn, lane, segs, list, layers,
                                    layer_base, sminb, n_slow);
          }
          __syncwarp();
