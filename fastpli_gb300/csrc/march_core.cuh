@@ -610,9 +610,13 @@ __device__ __forceinline__ void march_one_ray_column(const MarchParams &P, int64
 //      the interpolated axis — the interpolated axis of a step depends only on
 //      its position, not on the state;
 //   3. every lane applies its steps' rotations and attenuations in order.
-// The arithmetic per step is the same as march_one_ray's.
+// The arithmetic per step is the same as march_one_ray's.  Windows of 4 steps
+// keep the scratch at 17 KB per 128-thread block: the march lives on L1 hits
+// of its 8-corner gathers, and shared memory comes out of the same 256 KB
+// (8-step windows: 2.30 ms for config 2's five tilts, 4 steps: 2.12 ms,
+// 2 steps: 2.43 ms, the compaction then having too few jobs to fill warps).
 // ----------------------------------------------------------------------------
-constexpr int kCoopSteps = 8;
+constexpr int kCoopSteps = 4;
 constexpr int kCoopSlots = kCoopSteps * 32; // per warp
 constexpr int kCoopFields = 8;
 
@@ -623,14 +627,6 @@ struct CoopScratch {
 
 // job status codes written to field 4
 constexpr int kJobRotate = 0, kJobIdentity = 1, kJobZero = 2, kJobNorm = 4;
-
-// One out-of-line copy of the pairwise interpolation for the cooperative job
-// (up to seven calls per job; inlining them all overflows the instruction
-// cache).
-template <int MODE>
-__device__ __noinline__ F3 interp_axis_call(F3 v, F3 u, float t) {
-   return interp_axis<MODE>(v, u, t);
-}
 
 template <int MODE, bool TILT, bool WIDE>
 __device__ __forceinline__ void coop_job(const MarchParams &P, const int32_t *__restrict__ label,
@@ -667,22 +663,22 @@ __device__ __forceinline__ void coop_job(const MarchParams &P, const int32_t *__
       }
       F3 c00 = c[0], c10 = c[2], c01 = c[4], c11 = c[6];
       if (ax) {
-         c00 = interp_axis_call<MODE>(c[0], c[1], xd);
+         c00 = interp_axis<MODE>(c[0], c[1], xd);
          if (az)
-            c01 = interp_axis_call<MODE>(c[4], c[5], xd);
+            c01 = interp_axis<MODE>(c[4], c[5], xd);
          if (ay) {
-            c10 = interp_axis_call<MODE>(c[2], c[3], xd);
+            c10 = interp_axis<MODE>(c[2], c[3], xd);
             if (az)
-               c11 = interp_axis_call<MODE>(c[6], c[7], xd);
+               c11 = interp_axis<MODE>(c[6], c[7], xd);
          }
       }
       F3 c0 = c00, c1 = c01;
       if (ay) {
-         c0 = interp_axis_call<MODE>(c00, c10, yd);
+         c0 = interp_axis<MODE>(c00, c10, yd);
          if (az)
-            c1 = interp_axis_call<MODE>(c01, c11, yd);
+            c1 = interp_axis<MODE>(c01, c11, yd);
       }
-      v = az ? interp_axis_call<MODE>(c0, c1, zd) : c0;
+      v = az ? interp_axis<MODE>(c0, c1, zd) : c0;
    }
    int status;
    float c = 1.f, s = 0.f, cr = 1.f, sr = 0.f;

@@ -268,6 +268,9 @@ int plan_march(const fpgb_setup *s, const int64_t *dim, const double *props, int
    // with step 1 (simulator.cpp:259-261 then gives z = k + 1/2); at those
    // exact voxel centres Lerp and Slerp reduce to the voxel's own axis
    // (simulator.cpp:518-519)
+   // Lerp / Slerp: the warp-cooperative march (the faster variant on every
+   // volume measured; the batched path's autotuner may pick either)
+   P.coop = P.mode != 0 ? 1 : 0;
    P.column = 0;
    if (theta == 0 && P.n_z == P.Z && P.Z % 4 == 0 && step[0] == 0 && step[1] == 0) {
       bool seq = true;
@@ -312,9 +315,9 @@ int plan_march(const fpgb_setup *s, const int64_t *dim, const double *props, int
 // device
 // ======================================================================
 // 7 resident blocks per SM for the per-thread and column kernels (72
-// registers, a few bytes of spill: 3% faster than the 80-register default on
-// config 2; 8 blocks spill too much); the cooperative kernel keeps the 5 its
-// registers and 36 KB of shared scratch give it.
+// registers: 3% faster than the 80-register default on config 2; 8 blocks
+// spill too much); the cooperative kernel keeps the 5 its registers give it
+// (6 measured the same).
 template <int MODE, bool TILT, bool COOP, bool WIDE>
 __global__ void __launch_bounds__(128, COOP ? 5 : 7)
 march_rays(const MarchParams P, const int32_t *__restrict__ label,
