@@ -80,6 +80,10 @@ int pool_get(int slot, size_t bytes, void **ptr, cudaStream_t stream) {
 void prefault_host(void *p, size_t bytes) {
    if (!p || bytes < (size_t(8) << 20))
       return;
+   cudaPointerAttributes a;
+   if (cudaPointerGetAttributes(&a, p) == cudaSuccess && a.type == cudaMemoryTypeHost)
+      return; // page-locked: resident already
+   cudaGetLastError();
    const int64_t pg = (int64_t)sysconf(_SC_PAGESIZE);
    if (pg <= 0)
       return;

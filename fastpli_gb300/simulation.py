@@ -49,6 +49,31 @@ def _torch():
     return torch
 
 
+_TORCH_DTYPES = {np.dtype(np.int32): "int32", np.dtype(np.float32): "float32",
+                 np.dtype(np.float64): "float64"}
+
+
+_PINNED_MIN_BYTES = 8 << 20
+
+
+def _host_empty(shape, dtype):
+    """An uninitialised numpy array for an output of the host-buffer calls.
+    From 8 MiB up it lives in page-locked host memory: the device->host copy
+    into it runs at the link's rate with no page faulting, and an array passed
+    back in (the label / vector fields to run_simulation) is copied up at the
+    same rate.  That memory comes from torch's caching host allocator, so
+    arrays that are dropped return their blocks for the next call.  Either
+    way the result is an ordinary numpy array (its base keeps the block
+    alive)."""
+    shape = tuple(int(v) for v in shape)
+    dt = np.dtype(dtype)
+    if int(np.prod(shape)) * dt.itemsize < _PINNED_MIN_BYTES:
+        return np.empty(shape, dt)
+    torch = _torch()
+    t = torch.empty(shape, dtype=getattr(torch, _TORCH_DTYPES[dt]), pin_memory=True)
+    return t.numpy()
+
+
 def _stream_handle(stream):
     if stream is None:
         torch = _torch()
@@ -116,9 +141,9 @@ class _Generator:
         self._check()
         lib = N.load()
         X, Y, Z = (int(v) for v in self._dim)
-        label = np.empty((X, Y, Z), np.int32)
+        label = _host_empty((X, Y, Z), np.int32)
         vector = (np.zeros((0,), np.float32) if only_label
-                  else np.empty((X, Y, Z, 3), np.float32))
+                  else _host_empty((X, Y, Z, 3), np.float32))
         cap = self._flat.n_props
         props = np.zeros((cap, 2), np.float64)
         n_props = np.zeros(1, np.int64)
@@ -222,7 +247,8 @@ class _Simulator:
                              "!= label_field_.size()")
         if props.size % 2 != 0:
             raise ValueError("properties must be (n, 2)")
-        image = np.empty((int(d[0]), int(d[1]), self.n_rho), np.float64)
+        self.count_steps(d, theta, phi)  # setup / tilt errors before any allocation
+        image = _host_empty((int(d[0]), int(d[1]), self.n_rho), np.float64)
         w = N.Warnings()
         N.check(lib.fpgb_run_simulation(
             N.byref(self._setup.struct), N.ptr(d), N.ptr(label), N.ptr(vector),
