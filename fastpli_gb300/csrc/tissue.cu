@@ -451,7 +451,8 @@ size_t tissue_workspace_bytes(const TissuePlan &p) {
 
 int run_tissue(const TissuePlan &p, int only_label, int32_t *d_label,
                float *d_vector, void *d_ws, size_t ws_bytes,
-               unsigned long long **d_counters_out, cudaStream_t st) {
+               unsigned long long **d_counters_out, cudaStream_t st, int n_slabs,
+               int (*after_slab)(void *ctx, int64_t x0, int64_t x1), void *ctx) {
    const size_t need = tissue_workspace_bytes(p);
    if (ws_bytes < need) {
       set_error("generate_tissue: workspace %zu bytes < %zu needed", ws_bytes, need);
@@ -502,11 +503,78 @@ int run_tissue(const TissuePlan &p, int only_label, int32_t *d_label,
    auto *tile = reinterpret_cast<const TileDev *>(head);
    auto *lp = reinterpret_cast<int32_t *const *>(head + sizeof(TileDev));
    auto *vp = reinterpret_cast<float *const *>(head + sizeof(TileDev) + sizeof(void *));
+   // x-slabs of whole brick columns: bricks are numbered x-major, so a range
+   // of brick x indices is a contiguous brick range and a contiguous x range
+   // of voxels
+   struct Slabs {
+      int64_t bx[65];
+      int64_t X;
+      int (*after)(void *, int64_t, int64_t);
+      void *ctx;
+      static int thunk(void *self, int c) {
+         const Slabs &S = *static_cast<const Slabs *>(self);
+         const int64_t x0 = S.bx[c] * kBrickX, x1 = std::min(S.bx[c + 1] * kBrickX, S.X);
+         return S.after ? S.after(S.ctx, x0, x1) : FPGB_OK;
+      }
+   } slabs;
+   int64_t bound[65];
+   BrickChunks chunks{};
+   const int n = (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)n_slabs, 64, nb[0]}));
+   if (n > 1) {
+      slabs.X = p.X;
+      slabs.after = after_slab;
+      slabs.ctx = ctx;
+      for (int c = 0; c <= n; c++) {
+         slabs.bx[c] = nb[0] * c / n;
+         bound[c] = slabs.bx[c] * nb[1] * nb[2];
+      }
+      chunks = BrickChunks{n, bound, &Slabs::thunk, &slabs};
+   }
    FPGB_TRY(launch_voxel_bricks(segs, nullptr, (int64_t)p.segs.size(), tile, 1, n_bricks,
-                                p.brick_pairs, layers, p.n_bundles > 1, lp, vp, w, counters, st));
+                                p.brick_pairs, layers, p.n_bundles > 1, lp, vp, w, counters, st,
+                                n > 1 ? &chunks : nullptr));
+   if (n == 1 && after_slab)
+      FPGB_TRY(after_slab(ctx, 0, p.X));
    if (d_counters_out)
       *d_counters_out = counters;
    return FPGB_OK;
+}
+
+// Copies of finished x-slabs of a host-buffer generation (page-locked
+// outputs), queued on their own stream behind an event of the slab's launch.
+constexpr int kCopySlabs = 4;
+
+struct SlabCopy {
+   int32_t *label;
+   float *vector;
+   const int32_t *d_label;
+   const float *d_vector;
+   int64_t row; // voxels per x
+   cudaStream_t compute, copy;
+   std::vector<cudaEvent_t> events;
+
+   static int after(void *self, int64_t x0, int64_t x1) {
+      SlabCopy &S = *static_cast<SlabCopy *>(self);
+      cudaEvent_t ev;
+      FPGB_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+      S.events.push_back(ev);
+      FPGB_CUDA_TRY(cudaEventRecord(ev, S.compute));
+      FPGB_CUDA_TRY(cudaStreamWaitEvent(S.copy, ev, 0));
+      const int64_t v0 = x0 * S.row, nv = (x1 - x0) * S.row;
+      FPGB_CUDA_TRY(cudaMemcpyAsync(S.label + v0, S.d_label + v0, sizeof(int32_t) * nv,
+                                    cudaMemcpyDeviceToHost, S.copy));
+      if (S.vector)
+         FPGB_CUDA_TRY(cudaMemcpyAsync(S.vector + 3 * v0, S.d_vector + 3 * v0,
+                                       sizeof(float) * 3 * nv, cudaMemcpyDeviceToHost, S.copy));
+      return FPGB_OK;
+   }
+};
+
+static bool is_pinned(const void *p) {
+   cudaPointerAttributes a;
+   const bool pinned = cudaPointerGetAttributes(&a, p) == cudaSuccess && a.type == cudaMemoryTypeHost;
+   cudaGetLastError();
+   return pinned;
 }
 
 static int finish_props(const TissuePlan &p, double *props, int64_t props_cap,
@@ -596,17 +664,41 @@ int fpgb_generate_tissue(const fpgb_volume *vol, const fpgb_fibers *fibers, int 
    FPGB_TRY(pool_get(kSlotKeys, need, &d_ws));
    cudaStream_t st = nullptr;
    unsigned long long *d_counters = nullptr;
-   FPGB_TRY(run_tissue(p, only_label, (int32_t *)d_label, (float *)d_vec, d_ws, need,
-                       &d_counters, st));
-   // while the voxelizer runs
-   prefault_host(label, sizeof(int32_t) * nvox);
-   if (!only_label)
-      prefault_host(vector, sizeof(float) * 3 * nvox);
-   FPGB_CUDA_TRY(cudaMemcpyAsync(label, d_label, sizeof(int32_t) * nvox,
-                                 cudaMemcpyDeviceToHost, st));
-   if (!only_label)
-      FPGB_CUDA_TRY(cudaMemcpyAsync(vector, d_vec, sizeof(float) * 3 * nvox,
+   if (is_pinned(label) && (only_label || is_pinned(vector))) {
+      // page-locked outputs: each x-slab's rows are copied on a second stream
+      // while the next slabs are voxelized
+      SlabCopy sc;
+      sc.label = label;
+      sc.vector = only_label ? nullptr : vector;
+      sc.d_label = static_cast<const int32_t *>(d_label);
+      sc.d_vector = static_cast<const float *>(d_vec);
+      sc.row = p.Y * p.Z;
+      sc.compute = st;
+      FPGB_CUDA_TRY(cudaStreamCreateWithFlags(&sc.copy, cudaStreamNonBlocking));
+      int rc = run_tissue(p, only_label, (int32_t *)d_label, (float *)d_vec, d_ws, need,
+                          &d_counters, st, kCopySlabs, &SlabCopy::after, &sc);
+      const cudaError_t e = cudaStreamSynchronize(sc.copy);
+      for (cudaEvent_t ev : sc.events)
+         cudaEventDestroy(ev);
+      cudaStreamDestroy(sc.copy);
+      FPGB_TRY(rc);
+      if (e != cudaSuccess) {
+         set_error("generate_tissue: %s", cudaGetErrorString(e));
+         return FPGB_ECUDA;
+      }
+   } else {
+      FPGB_TRY(run_tissue(p, only_label, (int32_t *)d_label, (float *)d_vec, d_ws, need,
+                          &d_counters, st));
+      // while the voxelizer runs
+      prefault_host(label, sizeof(int32_t) * nvox);
+      if (!only_label)
+         prefault_host(vector, sizeof(float) * 3 * nvox);
+      FPGB_CUDA_TRY(cudaMemcpyAsync(label, d_label, sizeof(int32_t) * nvox,
                                     cudaMemcpyDeviceToHost, st));
+      if (!only_label)
+         FPGB_CUDA_TRY(cudaMemcpyAsync(vector, d_vec, sizeof(float) * 3 * nvox,
+                                       cudaMemcpyDeviceToHost, st));
+   }
    FPGB_TRY(finish_props(p, props, props_cap, n_props));
    fpgb_warnings tmp;
    FPGB_TRY(read_tissue_warnings(p, d_counters, warnings ? warnings : &tmp, st));

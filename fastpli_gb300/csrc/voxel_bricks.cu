@@ -499,7 +499,7 @@ __device__ __forceinline__ void radial_vector(const SegDev &S, int x, int y, int
 template <bool MULTI>
 __global__ void __launch_bounds__(kBrickThreads, 4)
 voxel_bricks(const SegDev *__restrict__ segs, const TileDev *__restrict__ tiles, int64_t n_tiles,
-             int64_t n_bricks, const unsigned *__restrict__ offsets,
+             int64_t brick_begin, int64_t brick_end, const unsigned *__restrict__ offsets,
              const unsigned *__restrict__ list, unsigned n_pairs,
              const LayerDev *__restrict__ layers,
              int32_t *const *__restrict__ labels, float *const *__restrict__ vecs,
@@ -510,7 +510,7 @@ voxel_bricks(const SegDev *__restrict__ segs, const TileDev *__restrict__ tiles,
    __shared__ unsigned s_next[2]; // next segment of the brick's list, per pass
    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
    unsigned long long n_slow = 0, n_overlap = 0, n_overflow = 0;
-   for (int64_t brick = blockIdx.x; brick < n_bricks; brick += gridDim.x) {
+   for (int64_t brick = brick_begin + blockIdx.x; brick < brick_end; brick += gridDim.x) {
       // tile of the brick: last tile whose brick_base <= brick
       int64_t lo = 0, hi = n_tiles - 1;
       while (lo < hi) {
@@ -643,9 +643,13 @@ int launch_voxel_bricks(const SegDev *segs, const int32_t *seg_tile, int64_t n_s
                         const TileDev *tiles, int64_t n_tiles, int64_t n_bricks, int64_t n_pairs,
                         const LayerDev *layers, bool multi_bundle, int32_t *const *labels,
                         float *const *vecs, void *ws, unsigned long long *counters,
-                        cudaStream_t st) {
+                        cudaStream_t st, const BrickChunks *chunks) {
    if (n_tiles <= 0 || n_bricks <= 0)
       return FPGB_OK;
+   if (chunks && (chunks->n < 1 || chunks->bound[0] != 0 || chunks->bound[chunks->n] != n_bricks)) {
+      set_error("voxelizer: brick chunks do not cover the bricks");
+      return FPGB_EINVAL;
+   }
    if (n_pairs >= 0xFFFFFFFFll || n_segs >= 0xFFFFFFFFll) {
       set_error("voxelizer: %lld segment-brick pairs exceed the 32-bit lists",
                 (long long)n_pairs);
@@ -674,16 +678,25 @@ int launch_voxel_bricks(const SegDev *segs, const int32_t *seg_tile, int64_t n_s
                                          n_pairs, counters);
       FPGB_CUDA_TRY(cudaGetLastError());
    }
-   const unsigned grid = (unsigned)std::min<int64_t>(n_bricks, 0x7FFFFFFF);
-   if (multi_bundle)
-      voxel_bricks<true><<<grid, kBrickThreads, 0, st>>>(segs, tiles, n_tiles, n_bricks, offsets,
-                                                         list, (unsigned)n_pairs, layers, labels,
-                                                         vecs, counters);
-   else
-      voxel_bricks<false><<<grid, kBrickThreads, 0, st>>>(segs, tiles, n_tiles, n_bricks, offsets,
-                                                          list, (unsigned)n_pairs, layers, labels,
-                                                          vecs, counters);
-   FPGB_CUDA_TRY(cudaGetLastError());
+   const int n_launch = chunks ? chunks->n : 1;
+   for (int c = 0; c < n_launch; c++) {
+      const int64_t b0 = chunks ? chunks->bound[c] : 0;
+      const int64_t b1 = chunks ? chunks->bound[c + 1] : n_bricks;
+      if (b1 > b0) {
+         const unsigned grid = (unsigned)std::min<int64_t>(b1 - b0, 0x7FFFFFFF);
+         if (multi_bundle)
+            voxel_bricks<true><<<grid, kBrickThreads, 0, st>>>(segs, tiles, n_tiles, b0, b1,
+                                                               offsets, list, (unsigned)n_pairs,
+                                                               layers, labels, vecs, counters);
+         else
+            voxel_bricks<false><<<grid, kBrickThreads, 0, st>>>(segs, tiles, n_tiles, b0, b1,
+                                                                offsets, list, (unsigned)n_pairs,
+                                                                layers, labels, vecs, counters);
+         FPGB_CUDA_TRY(cudaGetLastError());
+      }
+      if (chunks && chunks->after)
+         FPGB_TRY(chunks->after(chunks->ctx, c));
+   }
    return FPGB_OK;
 }
 

@@ -43,14 +43,26 @@ int64_t segment_brick_pairs(const SegDev &S);
 // Device scratch of the voxelizer for n_bricks bricks and n_pairs pairs.
 size_t brick_workspace_bytes(int64_t n_bricks, int64_t n_pairs);
 
+// Brick ranges to voxelize as separate launches, in order: launch c covers
+// bricks [bound[c], bound[c + 1]), and after(ctx, c) runs on the host once it
+// is enqueued (to queue work that waits for those bricks, e.g. the copy of
+// their part of the output).
+struct BrickChunks {
+   int n;
+   const int64_t *bound; // n + 1 brick indices, bound[0] = 0, bound[n] = n_bricks
+   int (*after)(void *ctx, int chunk);
+   void *ctx;
+};
+
 // Bins the segments to bricks and voxelizes every tile.  labels[t] / vecs[t]
 // are the tile's output arrays (vecs[t] may be null: labels only).
 // seg_tile may be null when there is one tile.  `ws` holds
 // brick_workspace_bytes(n_bricks, n_pairs) bytes, 256-byte aligned.
+// `chunks` may be null: one launch over every brick.
 int launch_voxel_bricks(const SegDev *segs, const int32_t *seg_tile, int64_t n_segs,
                         const TileDev *tiles, int64_t n_tiles, int64_t n_bricks, int64_t n_pairs,
                         const LayerDev *layers, bool multi_bundle, int32_t *const *labels,
                         float *const *vecs, void *ws, unsigned long long *counters,
-                        cudaStream_t st);
+                        cudaStream_t st, const BrickChunks *chunks = nullptr);
 
 } // namespace fpgb
