@@ -77,13 +77,19 @@ int pool_get(int slot, size_t bytes, void **ptr, cudaStream_t stream) {
    return FPGB_OK;
 }
 
+bool host_pinned(const void *p) {
+   cudaPointerAttributes a;
+   const bool pinned =
+       p && cudaPointerGetAttributes(&a, p) == cudaSuccess && a.type == cudaMemoryTypeHost;
+   cudaGetLastError();
+   return pinned;
+}
+
 void prefault_host(void *p, size_t bytes) {
    if (!p || bytes < (size_t(8) << 20))
       return;
-   cudaPointerAttributes a;
-   if (cudaPointerGetAttributes(&a, p) == cudaSuccess && a.type == cudaMemoryTypeHost)
+   if (host_pinned(p))
       return; // page-locked: resident already
-   cudaGetLastError();
    const int64_t pg = (int64_t)sysconf(_SC_PAGESIZE);
    if (pg <= 0)
       return;

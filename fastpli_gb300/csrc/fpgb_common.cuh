@@ -75,6 +75,9 @@ int pool_release_all();
 // ~145 GB/s.  The bytes written are overwritten by the copy.  Buffers under
 // 8 MiB are left alone.
 void prefault_host(void *p, size_t bytes);
+// Whether host pointer p is page-locked (its copies run asynchronously at
+// the link's rate).
+bool host_pinned(const void *p);
 
 inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 

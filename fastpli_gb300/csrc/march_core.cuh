@@ -227,39 +227,65 @@ __device__ F3 axis_interp(const MarchParams &P, const int32_t *__restrict__ labe
    return c0;
 }
 
+// IEEE double add / multiply / divide, each rounded once: the device's _rn
+// intrinsics, the host's plain operators (its code is built without
+// contraction).
+__host__ __device__ __forceinline__ double dadd(double a, double b) {
+#ifdef __CUDA_ARCH__
+   return __dadd_rn(a, b);
+#else
+   return a + b;
+#endif
+}
+__host__ __device__ __forceinline__ double dmul(double a, double b) {
+#ifdef __CUDA_ARCH__
+   return __dmul_rn(a, b);
+#else
+   return a * b;
+#endif
+}
+__host__ __device__ __forceinline__ double ddiv(double a, double b) {
+#ifdef __CUDA_ARCH__
+   return __ddiv_rn(a, b);
+#else
+   return a / b;
+#endif
+}
+
 // Ray start in the reference's double operation order
-// (simulator.cpp:663-681, 735-736, 230-231); explicit _rn intrinsics keep
-// every product and sum separately rounded.
-__device__ __forceinline__ void ray_start(const MarchParams &P, int64_t cx, int64_t cy,
+// (simulator.cpp:663-681, 735-736, 230-231), every product and sum
+// separately rounded.  Host and device: the host bounds which voxels a range
+// of rays can reach.
+__host__ __device__ __forceinline__ void ray_start(const MarchParams &P, int64_t cx, int64_t cy,
                                           double &sx, double &sy) {
-   const double ex = __dadd_rn((double)cx, 0.5), ey = __dadd_rn((double)cy, 0.5);
+   const double ex = dadd((double)cx, 0.5), ey = dadd((double)cy, 0.5);
    if (P.untilt) {
-      sx = __dadd_rn(__dadd_rn(ex, -P.hshift[0]), P.hstep[0]);
-      sy = __dadd_rn(__dadd_rn(ey, -P.hshift[1]), P.hstep[1]);
+      sx = dadd(dadd(ex, -P.hshift[0]), P.hstep[0]);
+      sy = dadd(dadd(ey, -P.hshift[1]), P.hstep[1]);
       return;
    }
-   const double e = __dadd_rn(__dadd_rn(ex, -P.pc[0]), -P.pt[0]);
-   const double f = __dadd_rn(__dadd_rn(ey, -P.pc[1]), -P.pt[1]);
-   const double Ds = __dadd_rn(__dmul_rn(e, P.Dd), -__dmul_rn(f, P.B));
-   const double Dt = __dadd_rn(__dmul_rn(P.A, f), -__dmul_rn(P.C, e));
-   const double s = __ddiv_rn(Ds, P.D), t = __ddiv_rn(Dt, P.D);
+   const double e = dadd(dadd(ex, -P.pc[0]), -P.pt[0]);
+   const double f = dadd(dadd(ey, -P.pc[1]), -P.pt[1]);
+   const double Ds = dadd(dmul(e, P.Dd), -dmul(f, P.B));
+   const double Dt = dadd(dmul(P.A, f), -dmul(P.C, e));
+   const double s = ddiv(Ds, P.D), t = ddiv(Dt, P.D);
    double rel[3];
 #pragma unroll
    for (int i = 0; i < 3; i++) {
-      const double p = __dadd_rn(__dadd_rn(__dadd_rn(P.pc[i], P.pt[i]), __dmul_rn(P.p1[i], s)),
-                                 __dmul_rn(P.p2[i], t));
-      rel[i] = __dadd_rn(p, -P.pc[i]);
+      const double p = dadd(dadd(dadd(P.pc[i], P.pt[i]), dmul(P.p1[i], s)),
+                                 dmul(P.p2[i], t));
+      rel[i] = dadd(p, -P.pc[i]);
    }
    double tis[2];
 #pragma unroll
    for (int i = 0; i < 2; i++) {
-      double a = __dmul_rn(rel[0], P.rti[3 * i + 0]);
-      a = __dadd_rn(a, __dmul_rn(rel[1], P.rti[3 * i + 1]));
-      a = __dadd_rn(a, __dmul_rn(rel[2], P.rti[3 * i + 2]));
-      tis[i] = __dadd_rn(a, P.pc[i]);
+      double a = dmul(rel[0], P.rti[3 * i + 0]);
+      a = dadd(a, dmul(rel[1], P.rti[3 * i + 1]));
+      a = dadd(a, dmul(rel[2], P.rti[3 * i + 2]));
+      tis[i] = dadd(a, P.pc[i]);
    }
-   sx = __dadd_rn(__dadd_rn(tis[0], -P.shift[0]), P.hstep[0]);
-   sy = __dadd_rn(__dadd_rn(tis[1], -P.shift[1]), P.hstep[1]);
+   sx = dadd(dadd(tis[0], -P.shift[0]), P.hstep[0]);
+   sy = dadd(dadd(tis[1], -P.shift[1]), P.hstep[1]);
 }
 
 // floor(v * 2^frac_bits) computed exactly with integer operations on the

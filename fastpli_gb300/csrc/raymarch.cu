@@ -320,18 +320,19 @@ int plan_march(const fpgb_setup *s, const int64_t *dim, const double *props, int
 // (6 measured the same).
 template <int MODE, bool TILT, bool COOP, bool WIDE>
 __global__ void __launch_bounds__(128, COOP ? 5 : 7)
-march_rays(const MarchParams P, const int32_t *__restrict__ label,
+march_rays(const MarchParams P, int64_t unit0, const int32_t *__restrict__ label,
            const float *__restrict__ vec, double *__restrict__ image,
            double *__restrict__ epa_t, double *__restrict__ epa_d, double *__restrict__ epa_r,
            unsigned long long *__restrict__ counters) {
+   const int64_t unit = unit0 + blockIdx.x; // launches may cover a range of units
    if (!TILT && P.column) { // 128 consecutive vertical rays per block
-      const int64_t ray = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+      const int64_t ray = unit * (int64_t)blockDim.x + threadIdx.x;
       if (ray < P.X * P.Y)
          march_one_ray_column(P, ray, label, vec, image, epa_t, epa_d, epa_r, counters);
       return;
    }
    int64_t ray; // one 4 x 32 tile of rays per block (tile_ray)
-   const bool valid = tile_ray<MODE != 0 && COOP>(P, blockIdx.x, threadIdx.x, ray);
+   const bool valid = tile_ray<MODE != 0 && COOP>(P, unit, threadIdx.x, ray);
    if (MODE == 0 || !COOP) {
       if (valid)
          march_one_ray<MODE, TILT, WIDE>(P, ray, label, vec, image, epa_t, epa_d, epa_r,
@@ -384,11 +385,11 @@ int sm_count() {
 }
 } // namespace
 
-int launch_march(const MarchPlan &mp, const int32_t *d_label, const float *d_vec,
-                 double *d_image, double *d_t, double *d_d, double *d_r,
-                 void *d_tables, unsigned long long *d_counters, cudaStream_t st) {
-   MarchParams P = mp.prm;
-   // tables: lut then ztab, 256-byte aligned, in caller-provided device memory
+// The launch form of the plan: tables copied into caller-provided device
+// memory (lut then ztab, 256-byte aligned) and pointed to from P.
+static int prepare_march(const MarchPlan &mp, const int32_t *d_label, const float *d_vec,
+                         void *d_tables, cudaStream_t st, MarchParams &P) {
+   P = mp.prm;
    char *w = static_cast<char *>(d_tables);
    LabelOptics *lut = reinterpret_cast<LabelOptics *>(w);
    w += align_up(sizeof(LabelOptics) * mp.lut.size(), 256);
@@ -401,22 +402,41 @@ int launch_march(const MarchPlan &mp, const int32_t *d_label, const float *d_vec
    P.ztab = zt;
    if (reinterpret_cast<uintptr_t>(d_label) % 16 || reinterpret_cast<uintptr_t>(d_vec) % 16)
       P.column = 0;
-   const int64_t n_rays = P.X * P.Y;
-   const bool tilt = P.rotate || P.dx_fx != 0 || P.dy_fx != 0;
-   const unsigned grid =
-       (!tilt && P.column)
-           ? (unsigned)((n_rays + 127) / 128)
-           : (unsigned)(((P.X + kRayTileX - 1) / kRayTileX) * ((P.Y + kRayTileY - 1) / kRayTileY));
-   // separate kernels per march variant: the cooperative one holds 36 KB of
-   // shared scratch and more registers, which must not cap the occupancy of
-   // the per-thread one
+   return FPGB_OK;
+}
+
+static bool march_tilted(const MarchParams &P) {
+   return P.rotate || P.dx_fx != 0 || P.dy_fx != 0;
+}
+
+// Blocks of one march: 128 consecutive rays each on the column path, else
+// one 4 x 32 ray tile each (x-major: tile t holds pixel columns
+// 4 (t / ceil(Y / 32)) ..+3).
+static int64_t march_units(const MarchParams &P) {
+   if (!march_tilted(P) && P.column)
+      return (P.X * P.Y + 127) / 128;
+   return ((P.X + kRayTileX - 1) / kRayTileX) * ((P.Y + kRayTileY - 1) / kRayTileY);
+}
+
+// Launches blocks [u0, u1) of the march.
+static int launch_march_units(const MarchParams &P, const int32_t *d_label, const float *d_vec,
+                              double *d_image, double *d_t, double *d_d, double *d_r,
+                              unsigned long long *d_counters, int64_t u0, int64_t u1,
+                              cudaStream_t st) {
+   if (u1 <= u0)
+      return FPGB_OK;
+   const bool tilt = march_tilted(P);
+   const unsigned grid = (unsigned)(u1 - u0);
+   // separate kernels per march variant: the cooperative one holds shared
+   // scratch and more registers, which must not cap the occupancy of the
+   // per-thread one
 #define FPGB_LAUNCH(M, T, C)                                                               \
    if (narrow)                                                                              \
-      march_rays<M, T, C, false><<<grid, 128, 0, st>>>(P, d_label, d_vec, d_image, d_t, d_d, \
-                                                       d_r, d_counters);                     \
+      march_rays<M, T, C, false><<<grid, 128, 0, st>>>(P, u0, d_label, d_vec, d_image, d_t, \
+                                                       d_d, d_r, d_counters);                \
    else                                                                                     \
-      march_rays<M, T, C, true><<<grid, 128, 0, st>>>(P, d_label, d_vec, d_image, d_t, d_d,  \
-                                                      d_r, d_counters)
+      march_rays<M, T, C, true><<<grid, 128, 0, st>>>(P, u0, d_label, d_vec, d_image, d_t,  \
+                                                      d_d, d_r, d_counters)
    const bool coop = P.coop != 0;
    const bool narrow = march_narrow(P);
    switch (P.mode * 4 + (tilt ? 2 : 0) + (coop ? 1 : 0)) {
@@ -434,6 +454,51 @@ int launch_march(const MarchPlan &mp, const int32_t *d_label, const float *d_vec
 #undef FPGB_LAUNCH
    FPGB_CUDA_TRY(cudaGetLastError());
    return FPGB_OK;
+}
+
+int launch_march(const MarchPlan &mp, const int32_t *d_label, const float *d_vec,
+                 double *d_image, double *d_t, double *d_d, double *d_r,
+                 void *d_tables, unsigned long long *d_counters, cudaStream_t st) {
+   MarchParams P;
+   FPGB_TRY(prepare_march(mp, d_label, d_vec, d_tables, st, P));
+   return launch_march_units(P, d_label, d_vec, d_image, d_t, d_d, d_r, d_counters, 0,
+                             march_units(P), st);
+}
+
+// Voxel x range [lo, hi] that the rays of march blocks [u0, u1) can read:
+// exact on the column path; otherwise the start positions (affine in the
+// pixel) at the corners of the blocks' pixel rectangle and their ends after
+// n_z steps, widened by 2 voxels (interpolation neighbours, the fixed-point
+// step's rounding).
+static void march_units_x_range(const MarchParams &P, int64_t u0, int64_t u1, int64_t &lo,
+                                int64_t &hi) {
+   int64_t cx0, cx1;
+   if (!march_tilted(P) && P.column) {
+      cx0 = u0 * 128 / P.Y;
+      cx1 = (std::min(u1 * 128, P.X * P.Y) - 1) / P.Y;
+      lo = cx0;
+      hi = cx1;
+      return;
+   }
+   const int64_t nby = (P.Y + kRayTileY - 1) / kRayTileY;
+   cx0 = (u0 / nby) * kRayTileX;
+   cx1 = std::min(P.X - 1, ((u1 - 1) / nby) * kRayTileX + kRayTileX - 1);
+   const double dxd = std::ldexp((double)P.dx_fx, -P.frac_bits) * (double)(P.n_z > 0 ? P.n_z - 1 : 0);
+   double mn = INFINITY, mx = -INFINITY;
+   for (int64_t cx : {cx0, cx1})
+      for (int64_t cy : {(int64_t)0, P.Y - 1}) {
+         double sx, sy;
+         ray_start(P, cx, cy, sx, sy);
+         mn = std::min({mn, sx, sx + dxd});
+         mx = std::max({mx, sx, sx + dxd});
+      }
+   if (!(mn > -1e15 && mx < 1e15)) { // not finite: every slab
+      lo = 0;
+      hi = P.X - 1;
+      return;
+   }
+   lo = std::max<int64_t>(0, (int64_t)std::floor(mn) - 2);
+   hi = std::min<int64_t>(P.X - 1, (int64_t)std::floor(mx) + 2);
 }
 
 size_t march_table_bytes(const MarchPlan &mp) {
@@ -507,6 +572,96 @@ static int run_sim_planned(const MarchPlan &mp, const int32_t *d_label, const fl
    return FPGB_OK;
 }
 
+// Host-buffer march over page-locked label / vector fields: the volume goes
+// up in x-slabs on a second stream, and the rays are launched in chunks,
+// each as soon as every slab its rays can read (march_units_x_range) is on
+// the device, so most of the march runs under the copy.  Same kernels and
+// bits as the one-launch march.
+// Consecutive chunks that wait for the same slab go out as one launch: a
+// chunk alone fills a third of the GPU, and the chunks that need the last
+// slab would otherwise run one after another after the copy (measured on
+// config 2: 4 slabs / 8 single-chunk launches left 0.47 ms of march after
+// the 2.41 ms copy).
+constexpr int kUpSlabs = 8, kRayChunks = 32;
+
+static int run_sim_pipelined(const MarchPlan &mp, const int32_t *label, const float *vector,
+                             int32_t *d_label, float *d_vec, int64_t n_props, double *d_img,
+                             fpgb_warnings *warnings, cudaStream_t st) {
+   const int64_t X = mp.prm.X, row = mp.prm.Y * mp.prm.Z;
+   void *tables = nullptr, *counters = nullptr;
+   FPGB_TRY(pool_get(kSlotProps, march_table_bytes(mp), &tables, st));
+   FPGB_TRY(pool_get(kSlotCounters, sizeof(unsigned long long) * kCounterWords, &counters, st));
+   auto *cnt = static_cast<unsigned long long *>(counters);
+   FPGB_TRY(init_counters(cnt, st));
+   MarchParams P;
+   FPGB_TRY(prepare_march(mp, d_label, d_vec, tables, st, P));
+   cudaStream_t up = nullptr;
+   cudaEvent_t ev[kUpSlabs] = {};
+   int64_t slab_end[kUpSlabs];
+   int rc = FPGB_OK;
+   auto run = [&]() -> int {
+      FPGB_CUDA_TRY(cudaStreamCreateWithFlags(&up, cudaStreamNonBlocking));
+      // the slab copies must not start before the stream's earlier work
+      // (the previous call's march may still read these buffers)
+      FPGB_CUDA_TRY(cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming));
+      FPGB_CUDA_TRY(cudaEventRecord(ev[0], st));
+      FPGB_CUDA_TRY(cudaStreamWaitEvent(up, ev[0], 0));
+      for (int s = 0; s < kUpSlabs; s++) {
+         const int64_t x0 = X * s / kUpSlabs, x1 = X * (s + 1) / kUpSlabs;
+         slab_end[s] = x1;
+         if (x1 > x0) {
+            FPGB_CUDA_TRY(cudaMemcpyAsync(d_label + x0 * row, label + x0 * row,
+                                          sizeof(int32_t) * (x1 - x0) * row,
+                                          cudaMemcpyHostToDevice, up));
+            FPGB_CUDA_TRY(cudaMemcpyAsync(d_vec + 3 * x0 * row, vector + 3 * x0 * row,
+                                          sizeof(float) * 3 * (x1 - x0) * row,
+                                          cudaMemcpyHostToDevice, up));
+         }
+         if (s > 0)
+            FPGB_CUDA_TRY(cudaEventCreateWithFlags(&ev[s], cudaEventDisableTiming));
+         FPGB_CUDA_TRY(cudaEventRecord(ev[s], up));
+      }
+      const int64_t nu = march_units(P);
+      int waited = -1;
+      int64_t g0 = 0; // first unit of the pending launch
+      for (int c = 0; c < kRayChunks; c++) {
+         const int64_t u0 = nu * c / kRayChunks, u1 = nu * (c + 1) / kRayChunks;
+         if (u1 <= u0)
+            continue;
+         int64_t lo, hi;
+         march_units_x_range(P, u0, u1, lo, hi);
+         int s = 0;
+         while (s < kUpSlabs - 1 && slab_end[s] <= hi)
+            s++;
+         s = std::max(s, waited);
+         if (s > waited && u0 > g0) { // launch the chunks that the slabs so far cover
+            FPGB_TRY(launch_march_units(P, d_label, d_vec, d_img, nullptr, nullptr, nullptr,
+                                        cnt, g0, u0, st));
+            g0 = u0;
+         }
+         if (s > waited) {
+            FPGB_CUDA_TRY(cudaStreamWaitEvent(st, ev[s], 0));
+            waited = s;
+         }
+      }
+      FPGB_TRY(launch_march_units(P, d_label, d_vec, d_img, nullptr, nullptr, nullptr, cnt, g0,
+                                  nu, st));
+      if (waited < kUpSlabs - 1)
+         FPGB_CUDA_TRY(cudaStreamWaitEvent(st, ev[kUpSlabs - 1], 0));
+      return launch_label_check(d_label, X * row, cnt, st);
+   };
+   rc = run();
+   if (up) {
+      cudaStreamSynchronize(up);
+      cudaStreamDestroy(up);
+   }
+   for (cudaEvent_t e : ev)
+      if (e)
+         cudaEventDestroy(e);
+   FPGB_TRY(rc);
+   return finish_counters(cnt, n_props, true, warnings, st);
+}
+
 static int run_sim_device(const fpgb_setup *setup, const int64_t *dim, const int32_t *d_label,
                           const float *d_vector, const double *props, int64_t n_props,
                           double theta, double phi, double *d_image, double *d_t, double *d_d,
@@ -571,14 +726,19 @@ int fpgb_run_simulation(const fpgb_setup *setup, const int64_t *dim, const int32
    FPGB_TRY(pool_get(kSlotImage, sizeof(double) * npix * setup->n_rho, &d_img));
    cudaStream_t st = nullptr;
    prefault_host(image, sizeof(double) * npix * setup->n_rho);
-   FPGB_CUDA_TRY(cudaMemcpyAsync(d_label, label, sizeof(int32_t) * nvox,
-                                 cudaMemcpyHostToDevice, st));
-   FPGB_CUDA_TRY(cudaMemcpyAsync(d_vec, vector, sizeof(float) * 3 * nvox,
-                                 cudaMemcpyHostToDevice, st));
    fpgb_warnings tmp;
-   FPGB_TRY(run_sim_planned(mp, (const int32_t *)d_label, (const float *)d_vec, n_props,
-                            (double *)d_img, nullptr, nullptr, nullptr,
-                            warnings ? warnings : &tmp, true, st));
+   if (host_pinned(label) && host_pinned(vector)) {
+      FPGB_TRY(run_sim_pipelined(mp, label, vector, (int32_t *)d_label, (float *)d_vec, n_props,
+                                 (double *)d_img, warnings ? warnings : &tmp, st));
+   } else {
+      FPGB_CUDA_TRY(cudaMemcpyAsync(d_label, label, sizeof(int32_t) * nvox,
+                                    cudaMemcpyHostToDevice, st));
+      FPGB_CUDA_TRY(cudaMemcpyAsync(d_vec, vector, sizeof(float) * 3 * nvox,
+                                    cudaMemcpyHostToDevice, st));
+      FPGB_TRY(run_sim_planned(mp, (const int32_t *)d_label, (const float *)d_vec, n_props,
+                               (double *)d_img, nullptr, nullptr, nullptr,
+                               warnings ? warnings : &tmp, true, st));
+   }
    FPGB_CUDA_TRY(cudaMemcpyAsync(image, d_img, sizeof(double) * npix * setup->n_rho,
                                  cudaMemcpyDeviceToHost, st));
    FPGB_CUDA_TRY(cudaStreamSynchronize(st));

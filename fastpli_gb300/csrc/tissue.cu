@@ -570,13 +570,6 @@ struct SlabCopy {
    }
 };
 
-static bool is_pinned(const void *p) {
-   cudaPointerAttributes a;
-   const bool pinned = cudaPointerGetAttributes(&a, p) == cudaSuccess && a.type == cudaMemoryTypeHost;
-   cudaGetLastError();
-   return pinned;
-}
-
 static int finish_props(const TissuePlan &p, double *props, int64_t props_cap,
                         int64_t *n_props) {
    const int64_t n = (int64_t)p.props.size() / 2;
@@ -664,7 +657,7 @@ int fpgb_generate_tissue(const fpgb_volume *vol, const fpgb_fibers *fibers, int 
    FPGB_TRY(pool_get(kSlotKeys, need, &d_ws));
    cudaStream_t st = nullptr;
    unsigned long long *d_counters = nullptr;
-   if (is_pinned(label) && (only_label || is_pinned(vector))) {
+   if (host_pinned(label) && (only_label || host_pinned(vector))) {
       // page-locked outputs: each x-slab's rows are copied on a second stream
       // while the next slabs are voxelized
       SlabCopy sc;

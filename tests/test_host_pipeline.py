@@ -1,0 +1,81 @@
+"""The host-buffer calls on page-locked arrays take a pipelined path:
+run_generation voxelizes in x-slabs and copies each slab down while the next
+ones run; run_simulation copies the volume up in x-slabs and launches the
+rays in chunks as soon as the slabs they can reach are on the device.  Both
+must give exactly the bits of the plain paths: the device-resident calls and
+the host-buffer calls on ordinary (pageable) numpy arrays.
+
+The volume is large enough (label field > 8 MiB) for run_generation to hand
+out page-locked arrays; tilts up to 60 degrees make the rays cross many
+slabs."""
+
+import warnings
+
+import numpy as np
+import pytest
+
+from fastpli_gb300 import synth
+from fastpli_gb300.simulation import _Generator, _Simulator
+
+pytestmark = pytest.mark.gpu
+
+TILTS = [(0.0, 0.0), (5.5, 0.0), (5.5, 90.0), (30.0, 45.0), (60.0, 200.0), (45.0, 300.0)]
+
+
+def _volume():
+    w = synth.crossing(seed=7, n_per_bundle=250, dim=(176, 160, 96), n_points=20)
+    g = _Generator()
+    g.set_volume(w.dim, w.origin, w.voxel_size)
+    g.set_fiber_bundles(w.bundles, w.layers)
+    return w, g
+
+
+def _sim(interp, untilt, flip_z, voxel_size):
+    s = _Simulator()
+    s.set_pli_setup(1.0, 26000.0, voxel_size, 525.0, 1.0, interp, untilt, flip_z,
+                    np.deg2rad([0.0, 30.0, 60.0, 90.0, 120.0, 150.0]))
+    return s
+
+
+@pytest.fixture(scope="module")
+def volume(cuda):
+    torch = cuda
+    w, g = _volume()
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        lab, vec, props = g.run_generation()
+        d_lab, d_vec, d_props, _ = g.run_generation_device()
+    torch.cuda.synchronize()
+    return w, lab, vec, props, d_lab, d_vec
+
+
+def test_generation_outputs_are_page_locked_and_match_device(volume, cuda):
+    torch = cuda
+    w, lab, vec, props, d_lab, d_vec = volume
+    # the arrays are numpy arrays backed by page-locked memory
+    assert isinstance(lab, np.ndarray) and isinstance(vec, np.ndarray)
+    assert torch.from_numpy(lab).is_pinned() and torch.from_numpy(vec).is_pinned()
+    assert np.array_equal(lab, d_lab.cpu().numpy())
+    assert np.array_equal(vec.view(np.uint32), d_vec.cpu().numpy().view(np.uint32))
+
+
+@pytest.mark.parametrize("interp,untilt,flip_z", [("Slerp", True, False), ("NN", False, True),
+                                                  ("Lerp", False, False)])
+def test_pipelined_march_matches_plain_paths(volume, cuda, interp, untilt, flip_z):
+    torch = cuda
+    w, lab, vec, props, d_lab, d_vec = volume
+    lab_pageable, vec_pageable = np.array(lab), np.array(vec)
+    assert not torch.from_numpy(lab_pageable).is_pinned()
+    sim = _sim(interp, untilt, flip_z, w.voxel_size)
+    for t, p in TILTS:
+        th, ph = np.deg2rad(t), np.deg2rad(p)
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            img_pipe = sim.run_simulation(w.dim, lab, vec, props, th, ph)
+            img_plain = sim.run_simulation(w.dim, lab_pageable, vec_pageable, props, th, ph)
+            img_dev = sim.run_simulation_device(w.dim, d_lab, d_vec, props, th, ph)
+        torch.cuda.synchronize()
+        assert np.all(np.isfinite(img_pipe))
+        assert np.array_equal(img_pipe.view(np.uint64), img_plain.view(np.uint64)), (t, p)
+        assert np.array_equal(img_pipe.view(np.uint64),
+                              img_dev.cpu().numpy().view(np.uint64)), (t, p)
