@@ -251,31 +251,46 @@ int plan_tissue(const fpgb_volume *vol, const fpgb_fibers *fb, TissuePlan *plan)
       set_error("generate_tissue: points == NULL");
       return FPGB_EINVAL;
    }
-   std::vector<double> xyz(3 * np), rad(np);
+   RawArray<double> xyz, rad;
+   xyz.reset((size_t)(3 * np));
+   rad.reset((size_t)np);
    const bool translate =
        vol->origin[0] != 0 || vol->origin[1] != 0 || vol->origin[2] != 0;
    const double f = 1.0 / vol->voxel_size;
-   for (int64_t i = 0; i < 4 * np; i++)
-      if (!std::isfinite(fb->points[i])) {
-         set_error("fiber point %lld is not finite", (long long)(i / 4));
-         return FPGB_EINVAL;
-      }
+   // first non-finite coordinate (points are checked, translated and scaled
+   // in parallel; the error names the lowest bad point as a serial scan would)
+   int64_t bad = INT64_MAX;
+#pragma omp parallel for schedule(static) reduction(min : bad)
    for (int64_t i = 0; i < np; i++) {
+      const double *q = fb->points + 4 * i;
+      if (!(std::isfinite(q[0]) && std::isfinite(q[1]) && std::isfinite(q[2]) &&
+            std::isfinite(q[3]))) {
+         bad = std::min(bad, i);
+         continue;
+      }
       for (int c = 0; c < 3; c++) {
-         double v = fb->points[4 * i + c];
+         double v = q[c];
          if (translate)
             v = v + (-vol->origin[c]);
          xyz[3 * i + c] = v * f;
       }
-      rad[i] = fb->points[4 * i + 3] * f;
+      rad[i] = q[3] * f;
    }
-   std::vector<Box> fbox(nf);
+   if (bad != INT64_MAX) {
+      set_error("fiber point %lld is not finite", (long long)bad);
+      return FPGB_EINVAL;
+   }
    for (int64_t fi = 0; fi < nf; fi++) {
       const int64_t p0 = fb->fiber_point_off[fi], p1 = fb->fiber_point_off[fi + 1];
       if (p1 < p0 || p1 > np) {
          set_error("generate_tissue: malformed fiber_point_off");
          return FPGB_EINVAL;
       }
+   }
+   std::vector<Box> fbox(nf);
+#pragma omp parallel for schedule(dynamic, 32)
+   for (int64_t fi = 0; fi < nf; fi++) {
+      const int64_t p0 = fb->fiber_point_off[fi], p1 = fb->fiber_point_off[fi + 1];
       fbox[fi] = fiber_box(xyz.data() + 3 * p0, rad.data() + p0, p1 - p0);
    }
    Box volbox;
