@@ -77,6 +77,14 @@ int pool_get(int slot, size_t bytes, void **ptr, cudaStream_t stream) {
    return FPGB_OK;
 }
 
+int &l2_end_state() {
+   static int state[64] = {};
+   int dev = 0;
+   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+      dev = 0;
+   return state[dev];
+}
+
 bool host_pinned(const void *p) {
    cudaPointerAttributes a;
    const bool pinned =

@@ -79,6 +79,11 @@ void prefault_host(void *p, size_t bytes);
 // the link's rate).
 bool host_pinned(const void *p);
 
+// Which x end of a volume the last device-resident pass on the current device
+// finished at (1 = high x, 0 = low x or unknown); the march starts there so
+// its first rays hit the part of the volume still in L2.  Performance only.
+int &l2_end_state();
+
 inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 inline cudaStream_t as_stream(void *s) {

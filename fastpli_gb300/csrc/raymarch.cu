@@ -324,7 +324,9 @@ march_rays(const MarchParams P, int64_t unit0, const int32_t *__restrict__ label
            const float *__restrict__ vec, double *__restrict__ image,
            double *__restrict__ epa_t, double *__restrict__ epa_d, double *__restrict__ epa_r,
            unsigned long long *__restrict__ counters) {
-   const int64_t unit = unit0 + blockIdx.x; // launches may cover a range of units
+   // launches may cover a range of units, in either order
+   const int64_t unit = P.reverse ? unit0 + (int64_t)gridDim.x - 1 - blockIdx.x
+                                  : unit0 + (int64_t)blockIdx.x;
    if (!TILT && P.column) { // 128 consecutive vertical rays per block
       const int64_t ray = unit * (int64_t)blockDim.x + threadIdx.x;
       if (ray < P.X * P.Y)
@@ -461,6 +463,11 @@ int launch_march(const MarchPlan &mp, const int32_t *d_label, const float *d_vec
                  void *d_tables, unsigned long long *d_counters, cudaStream_t st) {
    MarchParams P;
    FPGB_TRY(prepare_march(mp, d_label, d_vec, d_tables, st, P));
+   // start at the end of the volume the previous device-resident pass
+   // (voxelizer or march) finished at: that part is still in L2
+   int &end = l2_end_state();
+   P.reverse = end;
+   end = end ? 0 : 1;
    return launch_march_units(P, d_label, d_vec, d_image, d_t, d_d, d_r, d_counters, 0,
                              march_units(P), st);
 }

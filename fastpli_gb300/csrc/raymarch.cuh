@@ -62,7 +62,9 @@ struct MarchParams {
    // fits): the march reads a step's kind without a table load
    uint32_t kind_mask;
    int32_t kind_packed;
-   int32_t pad_;
+   // blocks run from the last unit down (the volume's high-x end first):
+   // the order only decides which rays go first, never a result
+   int32_t reverse;
 };
 static_assert(sizeof(MarchParams) % 16 == 0, "MarchParams is staged in 16-byte words");
 
