@@ -558,7 +558,7 @@ int run_tissue(const TissuePlan &p, int only_label, int32_t *d_label,
 
 // Copies of finished x-slabs of a host-buffer generation (page-locked
 // outputs), queued on their own stream behind an event of the slab's launch.
-constexpr int kCopySlabs = 4;
+constexpr int kCopySlabs = 8;
 
 struct SlabCopy {
    int32_t *label;
