@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cstdlib>
 #include <vector>
 
 #include "fpgb_common.cuh"
@@ -77,7 +78,13 @@ struct MarchPlan {
 
 // Whether the march may use 32-bit index arithmetic (MarchIdx<false>):
 // 3 X Y Z < 2^32 and ray positions below 2^30 voxels (frac_bits >= 32).
+// FPGB_WIDE_INDEX=1 in the environment forces the 64-bit kernels (which
+// every volume too large for the 32-bit ones uses) on any volume, so that
+// tests can check on small volumes that both give the same bits.
 inline bool march_narrow(const MarchParams &P) {
+   const char *w = std::getenv("FPGB_WIDE_INDEX");
+   if (w && w[0] == '1')
+      return false;
    return P.frac_bits >= 32 && P.X > 0 && P.Y > 0 && P.Z > 0 &&
           (double)P.X * (double)P.Y * (double)P.Z * 3.0 < 4294967296.0;
 }

@@ -54,11 +54,14 @@ def test_symbols_exported():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("coop", [0, 1])
-def test_batch_bit_identical_to_single_volume_path(cuda, coop):
-    """Either march variant of the batch (per-thread or warp-cooperative)
-    gives the single-volume path's bits."""
+@pytest.mark.parametrize("coop,wide", [(0, False), (1, False), (1, True)])
+def test_batch_bit_identical_to_single_volume_path(cuda, coop, wide, monkeypatch):
+    """Either march variant of the batch (per-thread or warp-cooperative),
+    with 32-bit or (forced, FPGB_WIDE_INDEX=1) 64-bit index arithmetic, gives
+    the single-volume path's bits."""
     torch = cuda
+    if wide:
+        monkeypatch.setenv("FPGB_WIDE_INDEX", "1")
     tiles = small_tiles()
     kw = tiles[0].setup_kwargs()
     b = B.TileBatch(tiles, kw, epa=True).allocate()

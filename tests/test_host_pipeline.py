@@ -79,3 +79,25 @@ def test_pipelined_march_matches_plain_paths(volume, cuda, interp, untilt, flip_
         assert np.array_equal(img_pipe.view(np.uint64), img_plain.view(np.uint64)), (t, p)
         assert np.array_equal(img_pipe.view(np.uint64),
                               img_dev.cpu().numpy().view(np.uint64)), (t, p)
+
+
+@pytest.mark.parametrize("interp", ["Slerp", "NN"])
+def test_wide_index_march_matches_narrow(volume, cuda, interp, monkeypatch):
+    """Volumes with 3 X Y Z >= 2^32 voxels march with 64-bit index arithmetic;
+    forced onto this volume (FPGB_WIDE_INDEX=1) those kernels give the bits of
+    the 32-bit ones (the batched path: tests/test_batch.py)."""
+    torch = cuda
+    w, lab, vec, props, d_lab, d_vec = volume
+    sim = _sim(interp, False, False, w.voxel_size)
+    for t, p in TILTS:
+        th, ph = np.deg2rad(t), np.deg2rad(p)
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            monkeypatch.delenv("FPGB_WIDE_INDEX", raising=False)
+            narrow = sim.run_simulation_device(w.dim, d_lab, d_vec, props, th, ph, epa=True)
+            monkeypatch.setenv("FPGB_WIDE_INDEX", "1")
+            wide = sim.run_simulation_device(w.dim, d_lab, d_vec, props, th, ph, epa=True)
+            monkeypatch.delenv("FPGB_WIDE_INDEX")
+        torch.cuda.synchronize()
+        for x, y in zip(narrow, wide):
+            assert torch.equal(x.view(torch.int64), y.view(torch.int64)), (t, p)
