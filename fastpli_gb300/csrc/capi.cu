@@ -77,8 +77,8 @@ int pool_get(int slot, size_t bytes, void **ptr, cudaStream_t stream) {
    return FPGB_OK;
 }
 
-int &l2_end_state() {
-   static int state[64] = {};
+std::atomic<int> &l2_end_state() {
+   static std::atomic<int> state[64] = {};
    int dev = 0;
    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
       dev = 0;

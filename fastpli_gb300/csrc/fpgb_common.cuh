@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdarg>
+#include <atomic>
 #include <cstdint>
 #include <cstdio>
 #include <string>
@@ -82,7 +83,7 @@ bool host_pinned(const void *p);
 // Which x end of a volume the last device-resident pass on the current device
 // finished at (1 = high x, 0 = low x or unknown); the march starts there so
 // its first rays hit the part of the volume still in L2.  Performance only.
-int &l2_end_state();
+std::atomic<int> &l2_end_state();
 
 inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 

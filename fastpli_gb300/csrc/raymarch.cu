@@ -465,9 +465,9 @@ int launch_march(const MarchPlan &mp, const int32_t *d_label, const float *d_vec
    FPGB_TRY(prepare_march(mp, d_label, d_vec, d_tables, st, P));
    // start at the end of the volume the previous device-resident pass
    // (voxelizer or march) finished at: that part is still in L2
-   int &end = l2_end_state();
-   P.reverse = end;
-   end = end ? 0 : 1;
+   std::atomic<int> &end = l2_end_state();
+   P.reverse = end.load(std::memory_order_relaxed);
+   end.store(P.reverse ? 0 : 1, std::memory_order_relaxed);
    return launch_march_units(P, d_label, d_vec, d_image, d_t, d_d, d_r, d_counters, 0,
                              march_units(P), st);
 }

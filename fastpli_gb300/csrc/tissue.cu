@@ -550,7 +550,7 @@ int run_tissue(const TissuePlan &p, int only_label, int32_t *d_label,
                                 n > 1 ? &chunks : nullptr));
    if (n == 1 && after_slab)
       FPGB_TRY(after_slab(ctx, 0, p.X));
-   l2_end_state() = 1; // bricks run x-major: the high-x end was written last
+   l2_end_state().store(1, std::memory_order_relaxed); // bricks run x-major: high x last
    if (d_counters_out)
       *d_counters_out = counters;
    return FPGB_OK;
