@@ -9,8 +9,10 @@
 * ``rofl(data, ...)`` — ROFL tilt analysis of one pixel's 5-tilt series
   (src/fastpli/analysis/rofl.py:16-63), and ``rofl_device`` for whole maps
   [5, X, Y, n_rho] (one warp per pixel in ``rofl.cu``).
+* ``fom_hsv_black(direction, inclination, mask)`` — the colour map of ROFL
+  results the pipelines return (images.py:22-56,156-186; numpy on the host).
 
-There is no CPU path: everything runs in the native library.
+epa and ROFL have no CPU path: they run in the native library.
 """
 
 import numpy as np
@@ -90,3 +92,30 @@ def rofl(data, tilt_angle=np.deg2rad(5.5), gain=3, dir_offset=0, grad_mode=False
     dev = torch.from_numpy(np.ascontiguousarray(data, np.float64)).cuda()[:, None, None, :]
     out = rofl_device(dev, tilt_angle, gain, dir_offset, grad_mode)
     return tuple(float(v) for v in out[0, 0].cpu().numpy())
+
+
+def fom_hsv_black(direction, inclination, mask=None):
+    """Fiber orientation map in the hsv_black colour space
+    (src/fastpli/analysis/images.py:22-56,156-186): hue 360 |direction| / pi,
+    value 1 - 2 |inclination| / pi, full saturation, as uint8 RGB
+    [X, Y, 3]; pixels outside ``mask`` black.  Host arrays (radians)."""
+    direction = np.asarray(direction, np.float64)
+    inclination = np.asarray(inclination, np.float64)
+    if mask is None:
+        mask = np.ones(direction.shape, bool)
+    mask = np.asarray(mask, bool)
+    h = (360.0 * np.abs(direction) / np.pi + 360) % 360
+    v = 1.0 - (2 * np.abs(inclination) / np.pi)
+    hi = np.floor(h / 60)
+    f = h / 60.0 - hi
+    p = np.zeros_like(v)  # v (1 - s), s = 1
+    q = v * (1 - f)
+    t = v * (1 - (1 - f))
+    # sector -> (r, g, b); sector 0 and any other value: (v, t, p)
+    r = np.select([hi == 1, hi == 2, hi == 3, hi == 4, hi == 5], [q, p, p, t, v], v)
+    g = np.select([hi == 1, hi == 2, hi == 3, hi == 4, hi == 5], [v, v, q, p, p], t)
+    b = np.select([hi == 1, hi == 2, hi == 3, hi == 4, hi == 5], [p, t, v, v, q], p)
+    rgb = np.stack([r * 255, g * 255, b * 255], -1).astype(np.int64)
+    out = np.zeros(direction.shape + (3,), np.uint8)
+    out[mask] = rgb[mask].astype(np.uint8)
+    return out

@@ -1,15 +1,15 @@
-"""A minimal read-only HDF5 reader, enough for the reference's golden
-regression file (tests/simulation/simpli_rep.h5, written by h5py): superblock
-version 0, version-1 object headers, groups stored as symbol tables (version-1
-B-trees of symbol-table nodes plus a local heap of link names), datasets with
-contiguous or compact layout and integer or IEEE floating-point elements.
+"""A minimal read-only HDF5 reader, for files written by h5py with its
+default (earliest) format: superblock version 0, version-1 object headers,
+groups stored as symbol tables (version-1 B-trees of symbol-table nodes plus
+a local heap of link names), datasets with contiguous or compact layout and
+integer or IEEE floating-point elements.  Chunked / compressed datasets and
+newer structures raise ValueError.
 
 Written from the published HDF5 file-format specification (superblock,
 "TREE"/"SNOD"/"HEAP" structures, object header messages 0x0001 dataspace,
 0x0003 datatype, 0x0008 data layout, 0x0010 continuation, 0x0011 symbol
-table).  Test infrastructure only (h5py and libhdf5 are not installed here):
-tests/golden/make_rep_h5_golden.py reads the file with it and commits the
-datasets as a numpy fixture.
+table).  It lets fastpli_gb300.io load .h5 fiber-bundle files without h5py,
+and the tests read the reference's golden regression file with it.
 
     read_all(path) -> {"group/sub/dataset": numpy array, ...}
 """

@@ -3,8 +3,10 @@
 Mirrors the parts of ``fastpli.simulation.Simpli`` that drive the forward
 model (src/fastpli/simulation/simpli.py:18-187 and the property setters of
 src/fastpli/simulation/__simpli.py:97-430): volume and optics properties,
-``generate_tissue()``, ``run_simulation()``, ``apply_epa()`` and
-``memory_usage()``.  The compiled back ends are this package's ``_Generator``
+``generate_tissue()``, ``run_simulation()``, the optic and analysis stages,
+the tissue / simulation pipelines that write their results to an h5py file
+(simpli.py:189-510, duck-typed: any object with h5py's dataset interface)
+and ``memory_usage()``.  The compiled back ends are this package's ``_Generator``
 and ``_Simulator``.  Device-resident helpers (``*_device``) keep the tissue
 in HBM across tilts, which the host API cannot (each reference call re-passes
 the tissue from host memory).
@@ -430,6 +432,179 @@ class Simpli:
             noisy = optic.add_noise(resampled.cpu().numpy(), self._noise_model)
             return resampled, torch.from_numpy(np.asarray(noisy, np.float64)).to(resampled.device)
         return resampled, optic.add_noise(resampled, self._noise_model)
+
+    # ------------------------------------------------- pipelines and I/O ---
+    def _print(self, msg):
+        if self._verbose:
+            print(msg)
+
+    def save_parameter_h5(self, h5f, script=None):
+        """Parameters as attributes of an h5py file or group
+        (__simpli.py:450-460)."""
+        import sys
+        from . import __version__
+        h5f.attrs["fastpli/simpli"] = str(self.get_dict())
+        h5f.attrs["fastpli/version"] = __version__
+        h5f.attrs["fastpli/compiler"] = "nvcc sm_103a (fastpli_gb300)"
+        h5f.attrs["fastpli/libraries"] = "fastpli_gb300"
+        h5f.attrs["fastpli/pip_freeze"] = ""
+        h5f.attrs["fastpli/system"] = sys.version
+        if script:
+            h5f.attrs["script"] = script.encode().decode("ascii", "ignore")
+
+    def crop_tilt_pixel(self):
+        """Image pixels at each border the tilts can reach outside the
+        volume (simpli.py:245-261)."""
+        if not self._untilt_sensor_view:
+            raise ValueError("currently only for untilt_sensor_view=True")
+        if self._voxel_size is None:
+            raise ValueError("voxel_size is not set")
+        if self._pixel_size is None:
+            raise ValueError("pixel_size is not set")
+        if self._tilts is None:
+            raise ValueError("tilts are not set")
+        return int(np.ceil(np.tan(np.max(np.abs(self._tilts[:, 0]))) * self._dim[-1] / 2 *
+                           self._voxel_size / self._pixel_size))
+
+    def crop_tilt_voxel(self):
+        """crop_tilt_pixel in voxels (simpli.py:263-268)."""
+        return int(np.round(self.crop_tilt_pixel() * self._pixel_size / self._voxel_size))
+
+    def add_crop_tilt_halo(self):
+        """Widen the volume by the tilt halo (simpli.py:270-274)."""
+        d = self.crop_tilt_voxel()
+        self.dim_origin[:2] -= d * self.voxel_size
+        self.dim[:2] += 2 * d
+
+    def rm_crop_tilt_halo(self, data):
+        """Remove the halo from images (simpli.py:276-282)."""
+        d = self.crop_tilt_voxel()
+        if d == 0:
+            return data
+        return data[d:-d, d:-d, :]
+
+    def run_tissue_pipeline(self, h5f=None, script=None, save=("tissue", "optical_axis")):
+        """generate_tissue() with its results written to ``h5f`` (an h5py
+        file or anything with its create_dataset / item interface)
+        (simpli.py:189-243)."""
+        self._check_volume_input()
+        self._check_generation_input()
+        save = list(save)
+        if script:
+            self.save_parameter_h5(h5f, script)
+        if "all" in save or "simulation" in save:
+            save = save + ["tissue", "optical_axis"]
+        tissue, optical_axis, tissue_properties = self.generate_tissue()
+        if h5f and "tissue" in save:
+            dset = h5f.create_dataset("tissue/tissue", tissue.shape, dtype=np.uint16,
+                                      compression="gzip", compression_opts=1)
+            dset[:] = tissue
+        if h5f and "optical_axis" in save:
+            dset = h5f.create_dataset("tissue/optical_axis", optical_axis.shape,
+                                      dtype=np.float32, compression="gzip",
+                                      compression_opts=1)
+            dset[:] = optical_axis
+        if h5f and "tissue" in save:
+            h5f["tissue/properties"] = tissue_properties
+        return tissue, optical_axis, tissue_properties
+
+    def _rofl_tilts_ok(self):
+        tl = self._tilts
+        return not (np.any(tl[:, 1] != np.deg2rad([0, 0, 90, 180, 270])) or tl[0, 0] != 0 or
+                    np.any(tl[1:, 0] != tl[1, 0]))
+
+    def run_simulation_pipeline(self, tissue, optical_axis, tissue_properties, h5f=None,
+                                save=("data", "optic", "epa", "mask", "rofl"),
+                                crop_tilt=False, mp_pool=None):
+        """Every tilt: march, optic, epa; then the pseudo mask and ROFL, with
+        results written to ``h5f`` (simpli.py:284-438).  Returns
+        (tilting_stack, (rofl_direction, rofl_incl, rofl_t_rel), fom)."""
+        from . import analysis
+        save = list(save)
+        if "all" in save or "simulation" in save:
+            save = save + ["data", "resample", "optic", "epa", "mask", "rofl"]
+        if self._tilts is None:
+            raise ValueError("tilts is not set")
+        if self._optical_sigma is None:
+            raise ValueError("optical_sigma is not set")
+        flag_rofl = self._rofl_tilts_ok()
+        if not flag_rofl:
+            warnings.warn("Tilts not suitable for ROFL. Skipping analysis")
+
+        def put(name, value, theta=None, phi=None):
+            h5f[name] = value
+            if theta is not None:
+                h5f[name].attrs["theta"] = theta
+                h5f[name].attrs["phi"] = phi
+
+        stack = [None] * len(self._tilts)
+        for t, (theta, phi) in enumerate(self._tilts):
+            images = self.run_simulation(tissue, optical_axis, tissue_properties, theta, phi)
+            if crop_tilt:
+                images = self.rm_crop_tilt_halo(images)
+            if h5f and "data" in save:
+                put(f"simulation/data/{t}", images, theta, phi)
+            img_res, img_noise = self.apply_optic(images, mp_pool=mp_pool)
+            if h5f and "resample" in save:
+                put(f"simulation/resample/{t}", img_res, theta, phi)
+            if h5f and "optic" in save:
+                put(f"simulation/optic/{t}", img_noise, theta, phi)
+            if h5f and "epa" in save:
+                epa = self.apply_epa(img_noise)
+                for name, v in zip(("transmittance", "direction", "retardation"), epa):
+                    put(f"analysis/epa/{t}/{name}", v, theta, phi)
+            stack[t] = img_noise
+        if h5f and "mask" in save:
+            mask = np.sum(tissue, 2) > 0
+            mask = self.apply_optic_resample(1.0 * mask, mp_pool=mp_pool) > 0.1
+            h5f["simulation/optic/mask"] = np.uint8(mask)
+        stack = np.array(stack)
+        while stack.ndim < 4:
+            stack = np.expand_dims(stack, axis=-2)
+        rofl = (None,) * 3
+        conf = (None,) * 5
+        if flag_rofl:
+            d, i, tr, conf = self.apply_rofl(stack, mask=None, mp_pool=mp_pool)
+            rofl = (d, i, tr)
+        if h5f and flag_rofl and "rofl" in save:
+            h5f["analysis/rofl/direction"] = rofl[0]
+            h5f["analysis/rofl/inclination"] = rofl[1]
+            h5f["analysis/rofl/t_rel"] = rofl[2]
+        if h5f and flag_rofl and "rofl_conf" in save:
+            for name, v in zip(("direction_conf", "inclination_conf", "t_rel_conf", "func",
+                                "n_iter"), conf):
+                h5f[f"analysis/rofl/{name}"] = v
+        fom = analysis.fom_hsv_black(rofl[0], rofl[1]) if flag_rofl else None
+        return stack, rofl, fom
+
+    def run_pipeline(self, h5f=None, script=None,
+                     save=("tissue", "optical_axis", "data", "optic", "epa", "mask", "rofl"),
+                     crop_tilt=False, mp_pool=None):
+        """Tissue then simulation pipeline (simpli.py:440-510).  Returns
+        ((tissue, optical_axis, tissue_properties), tilting_stack,
+        (rofl_direction, rofl_incl, rofl_t_rel), fom)."""
+        save = list(save)
+        if "all" in save:
+            save = ["tissue", "optical_axis", "data", "optic", "epa", "mask", "rofl"]
+        if "tissue" in save:
+            save = save + ["tissue", "optical_axis"]
+        if "simulation" in save:
+            save = save + ["data", "optic", "epa", "mask", "rofl"]
+        self._check_volume_input()
+        self._check_generation_input()
+        self._check_simulation_input()
+        if self._tilts is None:
+            raise ValueError("tilts is not set")
+        if self._optical_sigma is None:
+            raise ValueError("optical_sigma is not set")
+        if h5f:
+            self.save_parameter_h5(h5f, script)
+        tissue, optical_axis, props = self.run_tissue_pipeline(h5f=h5f, script=script,
+                                                               save=save)
+        stack, rofl, fom = self.run_simulation_pipeline(tissue, optical_axis, props, h5f=h5f,
+                                                        save=save, crop_tilt=crop_tilt,
+                                                        mp_pool=mp_pool)
+        return (tissue, optical_axis, props), stack, rofl, fom
 
     def apply_epa_device(self, data, mask=None):
         """epa of a device image stack in FP64 (epa.py:9-45) -> (t, d, r)."""

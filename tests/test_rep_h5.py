@@ -3,8 +3,8 @@ tests/simulation/simpli_rep.h5 (made by its tests/simulation/simpli_rep.py:
 cube.dat fibers, 5 µm voxels, three layers, Slerp, 5 tilts, optic with a
 seeded noise, epa, ROFL; the reference's simpli_test.py h5diffs a rerun
 against it at 1e-5 relative).  The datasets are in
-tests/golden/simpli_rep_h5.npz (tests/golden/make_rep_h5_golden.py, a
-minimal HDF5 reader in tests/golden/hdf5_min.py: no h5py here).
+tests/golden/simpli_rep_h5.npz (tests/golden/make_rep_h5_golden.py, with the
+minimal HDF5 reader fastpli_gb300/h5read.py: no h5py here).
 
 CPU: the oracle reproduces the file's tissue and orientation field bit for
 bit, its pre-optic images within 1e-12, its epa maps within 1e-12 and the
@@ -51,10 +51,8 @@ def test_fixture_is_the_reference_file():
     (checked where the reference tree is present)."""
     if not os.path.exists(REF_H5):
         pytest.skip("reference tree not present")
-    import sys
-    sys.path.insert(0, cases.GOLDEN)
-    import hdf5_min
-    data = hdf5_min.read_all(REF_H5)
+    from fastpli_gb300 import h5read
+    data = h5read.read_all(REF_H5)
     g = h5()
     assert sorted(k.replace("/", ".") for k in data) == sorted(g.files)
     for k, v in data.items():
