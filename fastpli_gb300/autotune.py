@@ -29,12 +29,26 @@ def cache_path():
     return os.environ.get("FPGB_AUTOTUNE_CACHE", _DEFAULT)
 
 
+_MEMO = {}
+
+
 def _load():
+    """The cache file's contents, parsed again only when the file changed
+    (the server reads it for every batch it launches)."""
+    p = cache_path()
     try:
-        with open(cache_path()) as f:
-            return json.load(f)
-    except Exception:
+        st = os.stat(p)
+    except OSError:
         return {}
+    stamp = (p, st.st_mtime_ns, st.st_size)
+    if _MEMO.get("stamp") != stamp:
+        try:
+            with open(p) as f:
+                data = json.load(f)
+        except Exception:
+            data = {}
+        _MEMO.update(stamp=stamp, data=data)
+    return dict(_MEMO["data"])
 
 
 def _store(d):

@@ -191,12 +191,17 @@ class TileBatch:
         return self._view(self.image_off[p], X * Y * self.n_rho, torch.float64,
                           (X, Y, self.n_rho))
 
-    def epa_maps(self, p):
+    def epa_block(self, p):
+        """transmittance, direction, retardation of pair p as one
+        [3, X, Y] float64 device view."""
         import torch
         if not self.epa:
             raise ValueError("batch planned without epa")
         X, Y = (int(v) for v in self.tiles[self.pair_tile[p]].dim[:2])
-        e = self._view(self.epa_off[p], 3 * X * Y, torch.float64, (3, X, Y))
+        return self._view(self.epa_off[p], 3 * X * Y, torch.float64, (3, X, Y))
+
+    def epa_maps(self, p):
+        e = self.epa_block(p)
         return e[0], e[1], e[2]
 
     def pairs_of(self, t):

@@ -120,9 +120,9 @@ class GpuRunner:
             b.warnings(stream=stream)  # raises on a label range error
             for t, r in enumerate(reqs):
                 maps = []
-                for p in b.pairs_of(t):
-                    tt, dd, rr = b.epa_maps(p)
-                    maps.append((tt.cpu().numpy(), dd.cpu().numpy(), rr.cpu().numpy()))
+                for p in b.pairs_of(t):  # one copy per pair
+                    e = b.epa_block(p).cpu().numpy()
+                    maps.append((e[0], e[1], e[2]))
                 images = [b.image(p).clone() for p in b.pairs_of(t)] if self.keep_images else None
                 r.result = {"epa": maps, "images": images}
         b.close()
