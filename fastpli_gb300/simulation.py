@@ -69,7 +69,10 @@ def _host_empty(shape, dtype):
     dt = np.dtype(dtype)
     if int(np.prod(shape)) * dt.itemsize < _PINNED_MIN_BYTES:
         return np.empty(shape, dt)
-    torch = _torch()
+    try:
+        torch = _torch()
+    except ImportError:  # no torch: ordinary pageable memory (one-copy path)
+        return np.empty(shape, dt)
     t = torch.empty(shape, dtype=getattr(torch, _TORCH_DTYPES[dt]), pin_memory=True)
     return t.numpy()
 
