@@ -101,3 +101,27 @@ def test_wide_index_march_matches_narrow(volume, cuda, interp, monkeypatch):
         torch.cuda.synchronize()
         for x, y in zip(narrow, wide):
             assert torch.equal(x.view(torch.int64), y.view(torch.int64)), (t, p)
+
+
+def test_pipelined_march_rejects_bad_labels(volume, cuda):
+    """A label outside the property table raises, as on the one-copy path
+    (simulator.cpp:149-167), also when the volume goes up in slabs."""
+    w, lab, vec, props, d_lab, d_vec = volume
+    sim = _sim("Slerp", True, False, w.voxel_size)
+    bad = _host_empty_like(lab)
+    bad[...] = lab
+    bad[w.dim[0] - 1, 3, 4] = props.shape[0] + 5  # in the last slab
+    with pytest.raises(ValueError, match="label"):
+        sim.run_simulation(w.dim, bad, vec, props, np.deg2rad(5.5), 0.0)
+    bad[...] = lab
+    bad[0, 0, 0] = -1
+    with pytest.raises(ValueError, match="label"):
+        sim.run_simulation(w.dim, bad, vec, props, np.deg2rad(5.5), 0.0)
+
+
+def _host_empty_like(a):
+    from fastpli_gb300.simulation import _host_empty
+    out = _host_empty(a.shape, a.dtype)
+    import torch
+    assert torch.from_numpy(out).is_pinned()
+    return out
