@@ -487,6 +487,7 @@ class Simpli:
         """generate_tissue() with its results written to ``h5f`` (an h5py
         file or anything with its create_dataset / item interface)
         (simpli.py:189-243)."""
+        self._print("Run tissue pipeline")
         self._check_volume_input()
         self._check_generation_input()
         save = list(save)
@@ -520,6 +521,7 @@ class Simpli:
         results written to ``h5f`` (simpli.py:284-438).  Returns
         (tilting_stack, (rofl_direction, rofl_incl, rofl_t_rel), fom)."""
         from . import analysis
+        self._print("Run simulation pipeline")
         save = list(save)
         if "all" in save or "simulation" in save:
             save = save + ["data", "resample", "optic", "epa", "mask", "rofl"]
@@ -539,6 +541,8 @@ class Simpli:
 
         stack = [None] * len(self._tilts)
         for t, (theta, phi) in enumerate(self._tilts):
+            self._print(f"Tilt {t}: theta: {np.rad2deg(theta):.1f} deg, phi: "
+                        f"{np.rad2deg(phi):.1f} deg")
             images = self.run_simulation(tissue, optical_axis, tissue_properties, theta, phi)
             if crop_tilt:
                 images = self.rm_crop_tilt_halo(images)
@@ -583,6 +587,7 @@ class Simpli:
         """Tissue then simulation pipeline (simpli.py:440-510).  Returns
         ((tissue, optical_axis, tissue_properties), tilting_stack,
         (rofl_direction, rofl_incl, rofl_t_rel), fom)."""
+        self._print("Run pipeline")
         save = list(save)
         if "all" in save:
             save = ["tissue", "optical_axis", "data", "optic", "epa", "mask", "rofl"]
