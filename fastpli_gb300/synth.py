@@ -13,6 +13,12 @@ the forward-model workloads:
 * ``watson``       — 1024x1024x240 at 0.1 µm, 20000 fibers x 50 points along
                      Watson(kappa=5) axes about a random axis, radii
                      lognormal(ln 0.8, 0.25), three layers.
+* ``wide_strip``   — 5504x16384x16 at 1 µm (1.44e9 voxels, past the 32-bit
+                     index range of the march), two bundles of 5 wavy fibers
+                     along y confined to the last 32 x-columns (radius
+                     U(1.5, 2.5) µm), layers (0.333, -0.004, 10, 'p'),
+                     (0.666, 0, 5, 'b'), (1.0, 0.004, 1, 'r'); tilts (0, 0)
+                     and 10° at phi = 90°.
 * ``tiles``        — 256 independent tiles, xy side U{64..512}, z U{30..120} at
                      0.2 µm, 50-2000 fibers with uniform directions, per-tile
                      dn U[-0.004, 0.004] and mu U[0, 20].
@@ -161,6 +167,33 @@ def watson(seed=3, n_fibers=20000, dim=(1024, 1024, 240), n_points=50):
     lys = [(0.6, 0.0, 5.0, "b"), (0.8, -0.002, 8.0, "p"), (1.0, 0.004, 10.0, "r")]
     X, Y, Z = dim
     return Workload(f"watson {X}x{Y}x{Z}", dim, vs, [fibers], [lys])
+
+
+WIDE_DIM = (5504, 16384, 16)
+WIDE_STRIP = 32  # the fibers lie in x >= WIDE_DIM[0] - WIDE_STRIP
+
+
+def wide_strip(seed=41):
+    """A volume whose vector field is indexed past 2^32 (3 X Y Z > 2^32),
+    with all tissue in its last ``WIDE_STRIP`` x-columns, where the linear
+    index is largest."""
+    X, Y, Z = WIDE_DIM
+    x0 = X - WIDE_STRIP
+    rng = np.random.default_rng(seed)
+    ys = np.arange(-24.0, Y + 24.0, 48.0)
+    bundles = []
+    for _ in range(2):
+        fibers = []
+        for _ in range(5):
+            a, b = rng.uniform(0, 2 * np.pi, 2)
+            x = x0 + 16.0 + 5.0 * np.sin(ys / 310.0 + a) + rng.uniform(-0.5, 0.5, ys.size)
+            z = 8.0 + 3.0 * np.sin(ys / 530.0 + b) + rng.uniform(-0.5, 0.5, ys.size)
+            r = np.full(ys.size, rng.uniform(1.5, 2.5))
+            fibers.append(np.stack([x, ys, z, r], axis=1))
+        bundles.append(fibers)
+    lys = [(0.333, -0.004, 10.0, "p"), (0.666, 0.0, 5.0, "b"), (1.0, 0.004, 1.0, "r")]
+    return Workload(f"wide strip {X}x{Y}x{Z}", WIDE_DIM, 1.0, bundles, [lys, lys],
+                    tilts=np.deg2rad([(0, 0), (10, 90)]))
 
 
 def tile(i, seed_base=1000, n_fibers=None, segment_um=2.0):
