@@ -589,12 +589,23 @@ static int run_sim_planned(const MarchPlan &mp, const int32_t *d_label, const fl
 // slab would otherwise run one after another after the copy (measured on
 // config 2: 4 slabs / 8 single-chunk launches left 0.47 ms of march after
 // the 2.41 ms copy).
+// With a page-locked host image, the image rows each launch completes go
+// down on a third stream while the later launches run, so only the last
+// launch's rows are copied after the march.
 constexpr int kUpSlabs = 8, kRayChunks = 32;
+
+// Image rows (pixel columns x) every ray of which lies in blocks [0, u).
+static int64_t march_units_rows_done(const MarchParams &P, int64_t u) {
+   if (!march_tilted(P) && P.column)
+      return std::min(P.X, u * 128 / P.Y);
+   return std::min(P.X, (u / ((P.Y + kRayTileY - 1) / kRayTileY)) * kRayTileX);
+}
 
 static int run_sim_pipelined(const MarchPlan &mp, const int32_t *label, const float *vector,
                              int32_t *d_label, float *d_vec, int64_t n_props, double *d_img,
-                             fpgb_warnings *warnings, cudaStream_t st) {
+                             double *h_image, fpgb_warnings *warnings, cudaStream_t st) {
    const int64_t X = mp.prm.X, row = mp.prm.Y * mp.prm.Z;
+   const int64_t img_row = mp.prm.Y * mp.prm.n_rho; // doubles per image row
    void *tables = nullptr, *counters = nullptr;
    FPGB_TRY(pool_get(kSlotProps, march_table_bytes(mp), &tables, st));
    FPGB_TRY(pool_get(kSlotCounters, sizeof(unsigned long long) * kCounterWords, &counters, st));
@@ -602,12 +613,30 @@ static int run_sim_pipelined(const MarchPlan &mp, const int32_t *label, const fl
    FPGB_TRY(init_counters(cnt, st));
    MarchParams P;
    FPGB_TRY(prepare_march(mp, d_label, d_vec, tables, st, P));
-   cudaStream_t up = nullptr;
+   cudaStream_t up = nullptr, down = nullptr;
    cudaEvent_t ev[kUpSlabs] = {};
+   cudaEvent_t done[kRayChunks + 1] = {};
+   int n_done = 0;
+   int64_t rows_copied = 0;
    int64_t slab_end[kUpSlabs];
    int rc = FPGB_OK;
+   // after a launch: copy the image rows [rows_copied, r1) it completed
+   auto copy_rows = [&](int64_t r1) -> int {
+      if (!h_image || r1 <= rows_copied)
+         return FPGB_OK;
+      FPGB_CUDA_TRY(cudaEventCreateWithFlags(&done[n_done], cudaEventDisableTiming));
+      FPGB_CUDA_TRY(cudaEventRecord(done[n_done], st));
+      FPGB_CUDA_TRY(cudaStreamWaitEvent(down, done[n_done++], 0));
+      FPGB_CUDA_TRY(cudaMemcpyAsync(h_image + rows_copied * img_row, d_img + rows_copied * img_row,
+                                    sizeof(double) * (r1 - rows_copied) * img_row,
+                                    cudaMemcpyDeviceToHost, down));
+      rows_copied = r1;
+      return FPGB_OK;
+   };
    auto run = [&]() -> int {
       FPGB_CUDA_TRY(cudaStreamCreateWithFlags(&up, cudaStreamNonBlocking));
+      if (h_image)
+         FPGB_CUDA_TRY(cudaStreamCreateWithFlags(&down, cudaStreamNonBlocking));
       // the slab copies must not start before the stream's earlier work
       // (the previous call's march may still read these buffers)
       FPGB_CUDA_TRY(cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming));
@@ -644,6 +673,7 @@ static int run_sim_pipelined(const MarchPlan &mp, const int32_t *label, const fl
          if (s > waited && u0 > g0) { // launch the chunks that the slabs so far cover
             FPGB_TRY(launch_march_units(P, d_label, d_vec, d_img, nullptr, nullptr, nullptr,
                                         cnt, g0, u0, st));
+            FPGB_TRY(copy_rows(march_units_rows_done(P, u0)));
             g0 = u0;
          }
          if (s > waited) {
@@ -653,16 +683,21 @@ static int run_sim_pipelined(const MarchPlan &mp, const int32_t *label, const fl
       }
       FPGB_TRY(launch_march_units(P, d_label, d_vec, d_img, nullptr, nullptr, nullptr, cnt, g0,
                                   nu, st));
+      FPGB_TRY(copy_rows(X)); // every launch is done: all remaining rows
       if (waited < kUpSlabs - 1)
          FPGB_CUDA_TRY(cudaStreamWaitEvent(st, ev[kUpSlabs - 1], 0));
       return launch_label_check(d_label, X * row, cnt, st);
    };
    rc = run();
-   if (up) {
-      cudaStreamSynchronize(up);
-      cudaStreamDestroy(up);
-   }
+   for (cudaStream_t s : {up, down})
+      if (s) {
+         cudaStreamSynchronize(s);
+         cudaStreamDestroy(s);
+      }
    for (cudaEvent_t e : ev)
+      if (e)
+         cudaEventDestroy(e);
+   for (cudaEvent_t e : done)
       if (e)
          cudaEventDestroy(e);
    FPGB_TRY(rc);
@@ -735,8 +770,12 @@ int fpgb_run_simulation(const fpgb_setup *setup, const int64_t *dim, const int32
    prefault_host(image, sizeof(double) * npix * setup->n_rho);
    fpgb_warnings tmp;
    if (host_pinned(label) && host_pinned(vector)) {
+      // a page-locked image takes its rows as the launches complete them
+      double *rows = host_pinned(image) ? image : nullptr;
       FPGB_TRY(run_sim_pipelined(mp, label, vector, (int32_t *)d_label, (float *)d_vec, n_props,
-                                 (double *)d_img, warnings ? warnings : &tmp, st));
+                                 (double *)d_img, rows, warnings ? warnings : &tmp, st));
+      if (rows)
+         return FPGB_OK;
    } else {
       FPGB_CUDA_TRY(cudaMemcpyAsync(d_label, label, sizeof(int32_t) * nvox,
                                     cudaMemcpyHostToDevice, st));

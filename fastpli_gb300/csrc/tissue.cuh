@@ -100,14 +100,16 @@ struct TissuePlan {
 int plan_tissue(const fpgb_volume *vol, const fpgb_fibers *fb, TissuePlan *plan);
 size_t tissue_workspace_bytes(const TissuePlan &p);
 // Voxelizes the planned volume into d_label / d_vector on stream st.  With
-// n_slabs > 1 the bricks are voxelized in that many x-slabs, one launch each,
-// and after_slab(ctx, x0, x1) runs on the host as soon as the launch for
-// voxels x0 <= x < x1 is enqueued (their label and vector rows are
-// contiguous in the output, so their copy can start while later slabs run).
+// n_slabs > 1 the bricks are voxelized in that many x-slabs, one launch each
+// (alternating between st and `alt` when alt is given), and
+// after_slab(ctx, x0, x1, s) runs on the host as soon as the launch for
+// voxels x0 <= x < x1 is enqueued on stream s (their label and vector rows
+// are contiguous in the output, so their copy can start while later slabs
+// run).  Work queued on st afterwards sees every slab.
 int run_tissue(const TissuePlan &p, int only_label, int32_t *d_label, float *d_vector,
                void *d_ws, size_t ws_bytes, unsigned long long **d_counters_out,
                cudaStream_t st, int n_slabs = 1,
-               int (*after_slab)(void *ctx, int64_t x0, int64_t x1) = nullptr,
-               void *ctx = nullptr);
+               int (*after_slab)(void *ctx, int64_t x0, int64_t x1, cudaStream_t s) = nullptr,
+               void *ctx = nullptr, cudaStream_t alt = nullptr);
 
 } // namespace fpgb

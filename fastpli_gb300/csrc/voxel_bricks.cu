@@ -679,25 +679,45 @@ int launch_voxel_bricks(const SegDev *segs, const int32_t *seg_tile, int64_t n_s
       FPGB_CUDA_TRY(cudaGetLastError());
    }
    const int n_launch = chunks ? chunks->n : 1;
-   for (int c = 0; c < n_launch; c++) {
-      const int64_t b0 = chunks ? chunks->bound[c] : 0;
-      const int64_t b1 = chunks ? chunks->bound[c + 1] : n_bricks;
-      if (b1 > b0) {
-         const unsigned grid = (unsigned)std::min<int64_t>(b1 - b0, 0x7FFFFFFF);
-         if (multi_bundle)
-            voxel_bricks<true><<<grid, kBrickThreads, 0, st>>>(segs, tiles, n_tiles, b0, b1,
-                                                               offsets, list, (unsigned)n_pairs,
-                                                               layers, labels, vecs, counters);
-         else
-            voxel_bricks<false><<<grid, kBrickThreads, 0, st>>>(segs, tiles, n_tiles, b0, b1,
+   cudaStream_t alt = chunks && chunks->n > 1 ? chunks->alt : nullptr;
+   cudaEvent_t joined[2] = {};
+   auto launch_all = [&]() -> int {
+      if (alt) { // alt starts after the binning
+         FPGB_CUDA_TRY(cudaEventCreateWithFlags(&joined[0], cudaEventDisableTiming));
+         FPGB_CUDA_TRY(cudaEventRecord(joined[0], st));
+         FPGB_CUDA_TRY(cudaStreamWaitEvent(alt, joined[0], 0));
+      }
+      for (int c = 0; c < n_launch; c++) {
+         const int64_t b0 = chunks ? chunks->bound[c] : 0;
+         const int64_t b1 = chunks ? chunks->bound[c + 1] : n_bricks;
+         cudaStream_t s = (alt && (c & 1)) ? alt : st;
+         if (b1 > b0) {
+            const unsigned grid = (unsigned)std::min<int64_t>(b1 - b0, 0x7FFFFFFF);
+            if (multi_bundle)
+               voxel_bricks<true><<<grid, kBrickThreads, 0, s>>>(segs, tiles, n_tiles, b0, b1,
                                                                 offsets, list, (unsigned)n_pairs,
                                                                 layers, labels, vecs, counters);
-         FPGB_CUDA_TRY(cudaGetLastError());
+            else
+               voxel_bricks<false><<<grid, kBrickThreads, 0, s>>>(segs, tiles, n_tiles, b0, b1,
+                                                                 offsets, list, (unsigned)n_pairs,
+                                                                 layers, labels, vecs, counters);
+            FPGB_CUDA_TRY(cudaGetLastError());
+         }
+         if (chunks && chunks->after)
+            FPGB_TRY(chunks->after(chunks->ctx, c, s));
       }
-      if (chunks && chunks->after)
-         FPGB_TRY(chunks->after(chunks->ctx, c));
-   }
-   return FPGB_OK;
+      if (alt) { // st's later work sees every chunk
+         FPGB_CUDA_TRY(cudaEventCreateWithFlags(&joined[1], cudaEventDisableTiming));
+         FPGB_CUDA_TRY(cudaEventRecord(joined[1], alt));
+         FPGB_CUDA_TRY(cudaStreamWaitEvent(st, joined[1], 0));
+      }
+      return FPGB_OK;
+   };
+   const int rc = launch_all();
+   for (cudaEvent_t e : joined)
+      if (e)
+         cudaEventDestroy(e);
+   return rc;
 }
 
 } // namespace fpgb

@@ -44,14 +44,19 @@ int64_t segment_brick_pairs(const SegDev &S);
 size_t brick_workspace_bytes(int64_t n_bricks, int64_t n_pairs);
 
 // Brick ranges to voxelize as separate launches, in order: launch c covers
-// bricks [bound[c], bound[c + 1]), and after(ctx, c) runs on the host once it
-// is enqueued (to queue work that waits for those bricks, e.g. the copy of
-// their part of the output).
+// bricks [bound[c], bound[c + 1]), and after(ctx, c, s) runs on the host once
+// it is enqueued on stream s (to queue work that waits for those bricks, e.g.
+// the copy of their part of the output).  With `alt` set, odd chunks run on
+// alt: launches on one stream each wait for the previous launch's slowest
+// brick, and two streams let a chunk's last bricks share the GPU with the
+// next chunk's first (the chunks write disjoint outputs).  The stream passed
+// to launch_voxel_bricks waits for alt before it returns.
 struct BrickChunks {
    int n;
    const int64_t *bound; // n + 1 brick indices, bound[0] = 0, bound[n] = n_bricks
-   int (*after)(void *ctx, int chunk);
+   int (*after)(void *ctx, int chunk, cudaStream_t s);
    void *ctx;
+   cudaStream_t alt;
 };
 
 // Bins the segments to bricks and voxelizes every tile.  labels[t] / vecs[t]

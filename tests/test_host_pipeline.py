@@ -103,6 +103,32 @@ def test_wide_index_march_matches_narrow(volume, cuda, interp, monkeypatch):
             assert torch.equal(x.view(torch.int64), y.view(torch.int64)), (t, p)
 
 
+@pytest.mark.parametrize("interp,untilt", [("Slerp", True), ("NN", False)])
+def test_pipelined_march_page_locked_image(cuda, interp, untilt):
+    """An image of 8 MiB and more is page-locked, and the pipelined march
+    copies its rows down as each launch completes them.  446 x 418 pixels:
+    the last 4-row ray tile is partial, and 418 rows of 32 rays split the
+    chunk boundaries inside ray tiles.  Bits equal the device-resident
+    march's at every tilt (theta = 0 takes the column path)."""
+    torch = cuda
+    w = synth.crossing(seed=8, n_per_bundle=120, dim=(446, 418, 24), n_points=20)
+    g = _Generator()
+    g.set_volume(w.dim, w.origin, w.voxel_size)
+    g.set_fiber_bundles(w.bundles, w.layers)
+    sim = _sim(interp, untilt, False, w.voxel_size)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        lab, vec, props = g.run_generation()
+        d_lab, d_vec, _, _ = g.run_generation_device()
+        for t, p in TILTS:
+            th, ph = np.deg2rad(t), np.deg2rad(p)
+            img = sim.run_simulation(w.dim, lab, vec, props, th, ph)
+            ref = sim.run_simulation_device(w.dim, d_lab, d_vec, props, th, ph)
+            torch.cuda.synchronize()
+            assert torch.from_numpy(img).is_pinned()
+            assert np.array_equal(img.view(np.uint64), ref.cpu().numpy().view(np.uint64)), (t, p)
+
+
 def test_pipelined_march_rejects_bad_labels(volume, cuda):
     """A label outside the property table raises, as on the one-copy path
     (simulator.cpp:149-167), also when the volume goes up in slabs."""
