@@ -330,9 +330,8 @@ def run_gpu(args):
                                 sync_warnings=False)
         if ev:
             ev[1].record(stream)
-        for k, (t, p) in enumerate(w.tilts):
-            sim.run_simulation_device(w.dim, label, vector, props, float(t), float(p),
-                                      image=images[k], sync_warnings=False)
+        sim.run_tilts_device(w.dim, label, vector, props, w.tilts, images=images,
+                             sync_warnings=False)
         if ev:
             ev[2].record(stream)
 

@@ -84,6 +84,8 @@ _SIGS = {
                                    ctypes.c_int),
     "fpgb_run_simulation_epa_device": ([_P, _P, _P, _P, _P, _I64, _D, _D, _P, _P,
                                         _P, _P, _P, _P], ctypes.c_int),
+    "fpgb_run_simulations_device": ([_P, _P, _P, _P, _P, _I64, _I64, _P, _P, _P, _P, _P,
+                                     _P, _P, _P], ctypes.c_int),
     "fpgb_count_steps": ([_P, _P, _D, _D], ctypes.c_int64),
     "fpgb_optic_resample_size": ([_I64, _I64, _D, _P], ctypes.c_int),
     "fpgb_optic_filter_resample_device": ([_P, _I64, _I64, _I64, _D, _D, _P, _P],

@@ -30,6 +30,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "fpgb_common.cuh"
@@ -715,6 +716,34 @@ static int run_sim_device(const fpgb_setup *setup, const int64_t *dim, const int
                           check_all, st);
 }
 
+// The streams a multi-tilt call spreads its tilts over (per device, created
+// on first use and kept for the process), and the lock that keeps two
+// calls' work on them in one order: a tilt's tables live in the stream's
+// pool slot, so one call's uploads must not land between another call's
+// upload and march on the same stream.
+constexpr int kTiltStreams = 4;
+
+static std::mutex &tilt_issue_mutex() {
+   static std::mutex mu;
+   return mu;
+}
+
+static int tilt_streams(cudaStream_t *out) { // caller holds tilt_issue_mutex
+   static cudaStream_t streams[64][kTiltStreams] = {};
+   int dev = 0;
+   FPGB_CUDA_TRY(cudaGetDevice(&dev));
+   if (dev < 0 || dev >= 64) {
+      set_error("run_simulations: device %d out of range", dev);
+      return FPGB_EINVAL;
+   }
+   for (int i = 0; i < kTiltStreams; i++) {
+      if (!streams[dev][i])
+         FPGB_CUDA_TRY(cudaStreamCreateWithFlags(&streams[dev][i], cudaStreamNonBlocking));
+      out[i] = streams[dev][i];
+   }
+   return FPGB_OK;
+}
+
 } // namespace fpgb
 
 using namespace fpgb;
@@ -749,6 +778,82 @@ int fpgb_run_simulation_epa_device(const fpgb_setup *setup, const int64_t *dim,
                                    double *d_ret, fpgb_warnings *warnings, void *stream) {
    return run_sim_device(setup, dim, d_label, d_vector, props, n_props, theta, phi, d_image,
                          d_trans, d_dir, d_ret, warnings, false, as_stream(stream));
+}
+
+int fpgb_run_simulations_device(const fpgb_setup *setup, const int64_t *dim,
+                                const int32_t *d_label, const float *d_vector,
+                                const double *props, int64_t n_props, int64_t n_tilts,
+                                const double *theta, const double *phi, double *const *d_images,
+                                double *const *d_trans, double *const *d_dir,
+                                double *const *d_ret, fpgb_warnings *warnings, void *stream) {
+   if (n_tilts < 0 || (n_tilts > 0 && (!theta || !phi || !d_images))) {
+      set_error("run_simulations: null tilt or image arrays");
+      return FPGB_EINVAL;
+   }
+   if (!d_label || !d_vector) {
+      set_error("run_simulation: null label/vector buffer");
+      return FPGB_EINVAL;
+   }
+   // every tilt is planned (and its setup errors raised) before device work
+   std::vector<MarchPlan> plans((size_t)n_tilts);
+   for (int64_t k = 0; k < n_tilts; k++) {
+      FPGB_TRY(plan_march(setup, dim, props, n_props, theta[k], phi[k], &plans[k]));
+      if (!d_images[k]) {
+         set_error("run_simulation: null image buffer");
+         return FPGB_EINVAL;
+      }
+   }
+   if (n_tilts == 0)
+      return FPGB_OK;
+   cudaStream_t st = as_stream(stream);
+   void *counters = nullptr;
+   FPGB_TRY(pool_get(kSlotCounters, sizeof(unsigned long long) * kCounterWords * n_tilts,
+                     &counters, st));
+   auto *cnt = static_cast<unsigned long long *>(counters);
+   {
+      std::lock_guard<std::mutex> lk(tilt_issue_mutex());
+      cudaStream_t side[kTiltStreams];
+      FPGB_TRY(tilt_streams(side));
+      const int n_side = (int)std::min<int64_t>(n_tilts, kTiltStreams);
+      std::vector<cudaEvent_t> evs;
+      auto event_on = [&](cudaStream_t from, cudaStream_t to) -> int {
+         cudaEvent_t e;
+         FPGB_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+         evs.push_back(e);
+         FPGB_CUDA_TRY(cudaEventRecord(e, from));
+         FPGB_CUDA_TRY(cudaStreamWaitEvent(to, e, 0));
+         return FPGB_OK;
+      };
+      int joined = 0; // side streams that started after the caller's work
+      auto issue = [&]() -> int {
+         for (; joined < n_side; joined++)
+            FPGB_TRY(event_on(st, side[joined]));
+         for (int64_t k = 0; k < n_tilts; k++) {
+            cudaStream_t s = side[k % kTiltStreams];
+            void *tables = nullptr;
+            FPGB_TRY(pool_get(kSlotProps, march_table_bytes(plans[k]), &tables, s));
+            FPGB_TRY(init_counters(cnt + k * kCounterWords, s));
+            FPGB_TRY(launch_march(plans[k], d_label, d_vector, d_images[k],
+                                  d_trans ? d_trans[k] : nullptr, d_dir ? d_dir[k] : nullptr,
+                                  d_ret ? d_ret[k] : nullptr, tables, cnt + k * kCounterWords,
+                                  s));
+         }
+         return FPGB_OK;
+      };
+      int rc = issue();
+      // the caller's stream waits for whatever was queued, also after an error
+      for (int i = 0; i < joined; i++) {
+         const int j = event_on(side[i], st);
+         rc = rc == FPGB_OK ? j : rc;
+      }
+      for (cudaEvent_t e : evs)
+         cudaEventDestroy(e);
+      FPGB_TRY(rc);
+   }
+   if (warnings)
+      for (int64_t k = 0; k < n_tilts; k++)
+         FPGB_TRY(finish_counters(cnt + k * kCounterWords, n_props, false, &warnings[k], st));
+   return FPGB_OK;
 }
 
 int fpgb_run_simulation(const fpgb_setup *setup, const int64_t *dim, const int32_t *label,

@@ -639,10 +639,13 @@ class Simpli:
 
     def run_tilts_device(self, label, vector, tissue_properties, tilts=None,
                          epa=False, stream=None):
-        """All tilts of ``self.tilts`` on resident tissue -> list of results."""
+        """All tilts of ``self.tilts`` on resident tissue -> list of results
+        (the tilts' marches overlap on the GPU; each result is the one
+        run_simulation_device gives)."""
         tilts = self._tilts if tilts is None else np.array(tilts, ndmin=2)
         if tilts is None:
             raise ValueError("tilts not set")
-        return [self.run_simulation_device(label, vector, tissue_properties,
-                                           float(t), float(p), epa=epa, stream=stream)
-                for t, p in tilts]
+        self._check_volume_input()
+        self._init_pli_setup()
+        return self._sim.run_tilts_device(self._dim, label, vector, tissue_properties,
+                                          tilts, epa=epa, stream=stream)

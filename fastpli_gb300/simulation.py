@@ -20,6 +20,7 @@ Differences, all deliberate:
 and take an optional CUDA stream.
 """
 
+import ctypes
 import warnings
 
 import numpy as np
@@ -302,6 +303,61 @@ class _Simulator:
         if epa:
             return image, t, dd, r
         return image
+
+    def run_tilts_device(self, dim, label_field, vector_field, properties, tilts,
+                         images=None, epa=False, stream=None, sync_warnings=True):
+        """Every (theta, phi) of ``tilts`` on one device-resident volume, the
+        marches spread over the library's own streams (joined back to
+        ``stream``) so that one tilt's last rays share the GPU with the next
+        tilt's first.  Each result is the one run_simulation_device gives for
+        that tilt.  Returns a list with one image tensor per tilt, or
+        (image, t, d, r) per tilt when ``epa``; ``images`` may hold the
+        output tensors."""
+        self._need_setup()
+        torch = _torch()
+        lib = N.load()
+        d = self._dim(dim, None)
+        props = np.ascontiguousarray(properties, dtype=np.float64)
+        for t, dt in ((label_field, torch.int32), (vector_field, torch.float32)):
+            if not t.is_cuda or t.dtype != dt or not t.is_contiguous():
+                raise ValueError("label/vector must be contiguous CUDA tensors "
+                                 "of int32/float32")
+        n = int(np.prod(d))
+        if label_field.numel() != n or vector_field.numel() != 3 * n:
+            raise ValueError("label/vector sizes do not match dim")
+        tl = np.ascontiguousarray(np.asarray(tilts, np.float64).reshape(-1, 2))
+        k = tl.shape[0]
+        X, Y = int(d[0]), int(d[1])
+        dev = label_field.device
+        if images is None:
+            images = [torch.empty((X, Y, self.n_rho), dtype=torch.float64, device=dev)
+                      for _ in range(k)]
+        if len(images) != k or any(not im.is_cuda or im.dtype != torch.float64 or
+                                   not im.is_contiguous() or im.numel() != X * Y * self.n_rho
+                                   for im in images):
+            raise ValueError("images must be one contiguous float64 CUDA tensor "
+                             "[X, Y, n_rho] per tilt")
+        def ptrs(ts):  # a C array of device pointers
+            return (ctypes.c_void_p * k)(*[t.data_ptr() for t in ts])
+
+        epa_out = [None, None, None]
+        if epa:
+            epa_out = [[torch.empty((X, Y), dtype=torch.float64, device=dev) for _ in range(k)]
+                       for _ in range(3)]
+        epa_ptrs = [ptrs(e) if epa else None for e in epa_out]
+        theta = np.ascontiguousarray(tl[:, 0])
+        phi = np.ascontiguousarray(tl[:, 1])
+        w = (N.Warnings * max(k, 1))()
+        N.check(lib.fpgb_run_simulations_device(
+            N.byref(self._setup.struct), N.ptr(d), N.ptr(label_field), N.ptr(vector_field),
+            N.ptr(props), props.size // 2, k, N.ptr(theta), N.ptr(phi), ptrs(images),
+            *epa_ptrs, w if sync_warnings else None, _stream_handle(stream)))
+        if sync_warnings:
+            for i in range(k):
+                _emit(w[i].as_dict(), _SIM_WARN)
+        if epa:
+            return [(images[i], epa_out[0][i], epa_out[1][i], epa_out[2][i]) for i in range(k)]
+        return list(images)
 
     def count_steps(self, dim, theta=0.0, phi=0.0):
         """Ray-voxel steps one call marches (X*Y rays x steps per ray)."""

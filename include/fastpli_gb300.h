@@ -169,6 +169,25 @@ int fpgb_run_simulation_epa_device(const fpgb_setup *setup, const int64_t *dim,
                                    double *d_dir, double *d_ret,
                                    fpgb_warnings *warnings, void *stream);
 
+/* Several tilts of one device-resident volume: the same march as
+ * fpgb_run_simulation_epa_device for each (theta[k], phi[k]) into
+ * d_images[k] (and d_trans[k], d_dir[k], d_ret[k] when those arrays are
+ * given; any entry may be NULL), with the tilts spread over the library's
+ * own streams so that one tilt's last rays share the GPU with the next
+ * tilt's first, joined back to `stream`.  Replaces the per-tilt loop of
+ * run_simulation calls in Simpli.run_simulation_pipeline
+ * (src/fastpli/simulation/simpli.py:337-345).  warnings, when not NULL,
+ * has n_tilts entries and makes the call synchronise; with NULL it is
+ * asynchronous like fpgb_run_simulation_device. */
+int fpgb_run_simulations_device(const fpgb_setup *setup, const int64_t *dim,
+                                const int32_t *d_label, const float *d_vector,
+                                const double *props, int64_t n_props,
+                                int64_t n_tilts, const double *theta,
+                                const double *phi, double *const *d_images,
+                                double *const *d_trans, double *const *d_dir,
+                                double *const *d_ret, fpgb_warnings *warnings,
+                                void *stream);
+
 /* Number of ray-voxel steps one run_simulation call marches: X*Y rays times
  * the steps each takes (simulator.cpp:259-261), computed on the host. */
 int64_t fpgb_count_steps(const fpgb_setup *setup, const int64_t *dim,

@@ -195,6 +195,38 @@ def test_device_path_and_fused_epa(cuda, oracle_port):
         assert trel <= EPA_TOL and rrel <= EPA_TOL and derr <= EPA_TOL
 
 
+def test_tilts_on_streams_match_single_calls(cuda):
+    """run_tilts_device spreads the tilts of one resident volume over the
+    library's streams (7 tilts: the streams are shared).  Every image and
+    epa map is bit-identical to that tilt's own run_simulation_device call,
+    warnings come per tilt, and a label outside the property table raises."""
+    torch = cuda
+    gname, kw, tilts = cases.sim_cases()["cube-Slerp"]
+    g = _gold(f"gen_{gname}.npz")
+    sim = _simulator(kw)
+    lab = torch.from_numpy(g["label"]).cuda()
+    vec = torch.from_numpy(g["vector"]).cuda()
+    many = [tuple(t) for t in tilts] + [(np.deg2rad(30.0), np.deg2rad(45.0)),
+                                        (np.deg2rad(60.0), np.deg2rad(200.0))]
+    res = sim.run_tilts_device(lab.shape, lab, vec, g["props"], many, epa=True)
+    for k, (t, p) in enumerate(many):
+        one = sim.run_simulation_device(lab.shape, lab, vec, g["props"], t, p, epa=True)
+        for a, b in zip(res[k], one):
+            assert torch.equal(a.view(torch.int64), b.view(torch.int64)), k
+    plain = sim.run_tilts_device(lab.shape, lab, vec, g["props"], many)
+    assert all(torch.equal(a, r[0]) for a, r in zip(plain, res))
+    scaled = vec.clone()
+    scaled[lab > 0] *= 1.0001
+    with warnings.catch_warnings(record=True) as w:
+        warnings.simplefilter("always")
+        sim.run_tilts_device(lab.shape, lab, scaled, g["props"], many[:2])
+    assert sum("not normalized" in str(x.message) for x in w) == 2
+    with pytest.raises(ValueError, match="label"):
+        sim.run_tilts_device(lab.shape, lab, vec, g["props"][:2], many)
+    again = sim.run_tilts_device(lab.shape, lab, vec, g["props"], many[:1])
+    assert torch.equal(again[0], res[0][0])
+
+
 def test_axis_warnings(cuda):
     """simpli_test.py:327-358: no warning for unit axes, UserWarning for a
     1.0001-scaled axis and for a zero axis."""
