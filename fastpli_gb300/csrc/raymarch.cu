@@ -320,7 +320,7 @@ int plan_march(const fpgb_setup *s, const int64_t *dim, const double *props, int
 // spill too much); the cooperative kernel keeps the 5 its registers give it
 // (6 measured the same).
 template <int MODE, bool TILT, bool COOP, bool WIDE>
-__global__ void __launch_bounds__(128, COOP ? 5 : 7)
+__global__ void __launch_bounds__(128, COOP ? 6 : 7)
 march_rays(const MarchParams P, int64_t unit0, const int32_t *__restrict__ label,
            const float *__restrict__ vec, double *__restrict__ image,
            double *__restrict__ epa_t, double *__restrict__ epa_d, double *__restrict__ epa_r,
