@@ -128,9 +128,8 @@ class _Sink:
         return True
 
 
-@pytest.mark.gpu
-def test_run_pipeline_on_reference_regression(cuda):
-    g = np.load(os.path.join(cases.GOLDEN, "simpli_rep_h5.npz"))
+def _rep_simpli():
+    """The scenario of the reference's regression file (simpli_rep.py)."""
     s = Simpli()
     s.voxel_size = 5
     s.set_voi([-60] * 3, [60] * 3)
@@ -143,6 +142,34 @@ def test_run_pipeline_on_reference_regression(cuda):
     s.pixel_size = 20
     s.optical_sigma = 0.71
     s.tilts = np.deg2rad([(0, 0), (5.5, 0), (5.5, 90), (5.5, 180), (5.5, 270)])
+    return s
+
+
+@pytest.mark.gpu
+def test_simpli_tilts_device_on_reference_regression(cuda):
+    """Simpli.generate_tissue_device + run_tilts_device (the tilts overlapped
+    on the library's streams) reproduce the regression file's images within
+    1e-4, and each equals its own run_simulation_device call bit for bit."""
+    torch = cuda
+    g = np.load(os.path.join(cases.GOLDEN, "simpli_rep_h5.npz"))
+    s = _rep_simpli()
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        lab, vec, props = s.generate_tissue_device()
+        res = s.run_tilts_device(lab, vec, props)
+        assert len(res) == 5
+        for k, (t, p) in enumerate(s.tilts):
+            ref = g[f"simulation.data.{k}"]
+            img = res[k].cpu().numpy()
+            assert (np.abs(img - ref) / np.abs(ref)).max() < 1e-4, k
+            one = s.run_simulation_device(lab, vec, props, t, p)
+            assert torch.equal(res[k], one), k
+
+
+@pytest.mark.gpu
+def test_run_pipeline_on_reference_regression(cuda):
+    g = np.load(os.path.join(cases.GOLDEN, "simpli_rep_h5.npz"))
+    s = _rep_simpli()
     from fastpli_gb300 import optic
     s.noise_model = optic.NegativeBinomialNoise(3.0, seed=1)
     h5f = _Sink()
