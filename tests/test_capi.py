@@ -158,3 +158,29 @@ def test_stage_entry_points_validate_before_device_work():
     assert lib.fpgb_rofl_device(N.ptr(one), 1, 6, 0.1, 1.0, 0.0, 0, None, N.ptr(out), None,
                                 None) == N.FPGB_EINVAL
     assert b"gain" in lib.fpgb_last_error()
+
+
+def test_multi_tilt_entry_validates_before_device_work():
+    """fpgb_run_simulations_device refuses missing tilt arrays, a negative
+    tilt count and a tilt the setup rejects (theta = 90 deg: no positive z
+    step) with FPGB_EINVAL, and takes an empty tilt list as a no-op, all
+    before any CUDA call (runs without a GPU; the buffer addresses are never
+    dereferenced)."""
+    lib = N.load()
+    s = _setup()
+    dim = np.array([4, 4, 4], np.int64)
+    props = np.zeros((1, 2))
+    buf = np.zeros(4, np.int64)  # stands in for device buffers
+    imgs = (ctypes.c_void_p * 2)(buf.ctypes.data, buf.ctypes.data)
+
+    def call(n, theta, phi):
+        return lib.fpgb_run_simulations_device(
+            N.byref(s.struct), N.ptr(dim), N.ptr(buf), N.ptr(buf), N.ptr(props), 1, n,
+            N.ptr(theta), N.ptr(phi), imgs, None, None, None, None, None)
+
+    ph = np.zeros(2)
+    assert call(2, None, ph) == N.FPGB_EINVAL
+    assert call(-1, ph, ph) == N.FPGB_EINVAL
+    assert call(2, np.array([0.0, np.pi / 2]), ph) == N.FPGB_EINVAL
+    assert b"theta" in lib.fpgb_last_error()
+    assert call(0, None, None) == 0
