@@ -11,6 +11,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <utility>
 
 #include "fpgb_common.cuh"
@@ -34,16 +35,24 @@ struct PoolEntry {
    size_t bytes = 0;
 };
 std::mutex g_pool_mu;
+// A buffer is keyed by the calling host thread as well as by (device,
+// stream, slot): a call takes its buffers, then enqueues work into them after
+// the pool lock is dropped, so a buffer may only ever be replaced by the
+// thread that uses it.  Two threads on one stream (e.g. the legacy default
+// stream) therefore never free each other's buffers mid-call.
 struct PoolKey {
    int dev;
    uintptr_t stream;
    int slot;
+   std::thread::id thread;
    bool operator<(const PoolKey &o) const {
       if (dev != o.dev)
          return dev < o.dev;
       if (stream != o.stream)
          return stream < o.stream;
-      return slot < o.slot;
+      if (slot != o.slot)
+         return slot < o.slot;
+      return thread < o.thread;
    }
 };
 std::map<PoolKey, PoolEntry> g_pool;
@@ -53,11 +62,13 @@ int pool_get(int slot, size_t bytes, void **ptr, cudaStream_t stream) {
    int dev = 0;
    FPGB_CUDA_TRY(cudaGetDevice(&dev));
    std::lock_guard<std::mutex> lk(g_pool_mu);
-   PoolEntry &e = g_pool[PoolKey{dev, reinterpret_cast<uintptr_t>(stream), slot}];
+   PoolEntry &e =
+       g_pool[PoolKey{dev, reinterpret_cast<uintptr_t>(stream), slot, std::this_thread::get_id()}];
    if (e.bytes < bytes) {
       if (e.ptr) {
-         // Buffers of this slot may still be in use by work queued on any
-         // stream: wait for the device before giving the memory back.
+         // This thread's earlier calls may still have work queued on any
+         // stream that uses the buffer: wait for the device before giving
+         // the memory back.
          FPGB_CUDA_TRY(cudaDeviceSynchronize());
          FPGB_CUDA_TRY(cudaFree(e.ptr));
          e.ptr = nullptr;

@@ -63,8 +63,10 @@ enum PoolSlot : int {
    kSlotOptic,
    kNumSlots
 };
-// Buffers are cached per (device, stream, slot): concurrent calls on
-// different streams never share a buffer.
+// Buffers are cached per (device, stream, slot, host thread): concurrent
+// calls never share a buffer, and a buffer is only grown (freed and
+// re-allocated) by the thread that owns it.  pool_release_all frees every
+// buffer of the device and must not overlap other calls of the library.
 int pool_get(int slot, size_t bytes, void **ptr, cudaStream_t stream = nullptr);
 int pool_release_all();
 

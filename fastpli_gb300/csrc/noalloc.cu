@@ -92,7 +92,7 @@ extern "C" int fpgb_generate_tissue_noalloc(const fpgb_volume *vol, const fpgb_f
       return FPGB_EINVAL;
    }
    const int64_t rows = (int64_t)p.props.size() / 2;
-   if (props && props_cap < rows) {
+   if (props && props_cap < rows) { // refused before any device work
       set_error("props_cap %lld < %lld rows", (long long)props_cap, (long long)rows);
       return FPGB_EINVAL;
    }
@@ -102,17 +102,8 @@ extern "C" int fpgb_generate_tissue_noalloc(const fpgb_volume *vol, const fpgb_f
    unsigned long long *d_counters = nullptr;
    FPGB_TRY(run_tissue(p, only_label, d_label, d_vector, scratch, kNoAllocScratchBytes,
                        &d_counters, st));
-   if (n_props)
-      *n_props = rows;
-   if (props)
-      std::memcpy(props, p.props.data(), sizeof(double) * 2 * rows);
-   if (warnings) {
-      long long h[kCounterWords];
-      FPGB_CUDA_TRY(cudaMemcpyAsync(h, d_counters, sizeof h, cudaMemcpyDeviceToHost, st));
-      FPGB_CUDA_TRY(cudaStreamSynchronize(st));
-      warnings_from_counters(h, warnings);
-      warnings->overlap = warnings->overlap > 0 ? 1 : 0;
-      warnings->single_point = p.single_point;
-   }
-   return FPGB_OK;
+   // the same completion as fpgb_generate_tissue_device: props, then the
+   // warnings and the binning-overflow status from the counter block
+   FPGB_TRY(finish_props(p, props, props_cap, n_props));
+   return read_tissue_warnings(p, d_counters, warnings, st);
 }

@@ -592,8 +592,7 @@ struct SlabCopy {
    }
 };
 
-static int finish_props(const TissuePlan &p, double *props, int64_t props_cap,
-                        int64_t *n_props) {
+int finish_props(const TissuePlan &p, double *props, int64_t props_cap, int64_t *n_props) {
    const int64_t n = (int64_t)p.props.size() / 2;
    if (n_props)
       *n_props = n;
@@ -607,21 +606,27 @@ static int finish_props(const TissuePlan &p, double *props, int64_t props_cap,
    return FPGB_OK;
 }
 
-static int read_tissue_warnings(const TissuePlan &p, unsigned long long *d_counters,
-                                fpgb_warnings *w, cudaStream_t st) {
+int tissue_status_from_counters(const TissuePlan &p, const long long *h, fpgb_warnings *w) {
+   if (h[6] & kStatusOverflow) { // the device binning disagreed with the host plan
+      set_error("generate_tissue: internal error, segment-brick lists overflowed");
+      return FPGB_ECUDA;
+   }
+   if (!w)
+      return FPGB_OK;
+   warnings_from_counters(h, w);
+   w->overlap = w->overlap > 0 ? 1 : 0; // the reference warns once (generator.cpp:353-359)
+   w->single_point = p.single_point;
+   return FPGB_OK;
+}
+
+int read_tissue_warnings(const TissuePlan &p, unsigned long long *d_counters, fpgb_warnings *w,
+                         cudaStream_t st) {
    if (!w)
       return FPGB_OK;
    long long h[kCounterWords];
    FPGB_CUDA_TRY(cudaMemcpyAsync(h, d_counters, sizeof h, cudaMemcpyDeviceToHost, st));
    FPGB_CUDA_TRY(cudaStreamSynchronize(st));
-   if (h[6] & kStatusOverflow) { // the device binning disagreed with the host plan
-      set_error("generate_tissue: internal error, segment-brick lists overflowed");
-      return FPGB_ECUDA;
-   }
-   warnings_from_counters(h, w);
-   w->overlap = w->overlap > 0 ? 1 : 0; // the reference warns once (generator.cpp:353-359)
-   w->single_point = p.single_point;
-   return FPGB_OK;
+   return tissue_status_from_counters(p, h, w);
 }
 
 } // namespace fpgb

@@ -112,4 +112,20 @@ int run_tissue(const TissuePlan &p, int only_label, int32_t *d_label, float *d_v
                int (*after_slab)(void *ctx, int64_t x0, int64_t x1, cudaStream_t s) = nullptr,
                void *ctx = nullptr, cudaStream_t alt = nullptr);
 
+// Copies the planned (dn, mu) rows to props (host, props_cap rows) and their
+// count to n_props; either may be null.
+int finish_props(const TissuePlan &p, double *props, int64_t props_cap, int64_t *n_props);
+
+// Decodes a voxelizer counter block copied to the host (kCounterWords
+// words): FPGB_ECUDA, with the error set, when the device binning overflowed
+// the host plan's segment-brick lists; otherwise the reference's warnings
+// into w (when not null).
+int tissue_status_from_counters(const TissuePlan &p, const long long *h, fpgb_warnings *w);
+
+// Reads the voxelizer's counter block (synchronising st) into w: the
+// reference's warnings, or FPGB_ECUDA when the device binning overflowed the
+// host plan's segment-brick lists.  Does nothing when w is null.
+int read_tissue_warnings(const TissuePlan &p, unsigned long long *d_counters, fpgb_warnings *w,
+                         cudaStream_t st);
+
 } // namespace fpgb

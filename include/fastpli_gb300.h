@@ -101,8 +101,9 @@ int fpgb_generate_tissue(const fpgb_volume *vol, const fpgb_fibers *fibers,
 
 /* Device-resident variant.  d_label / d_vector are device buffers of the
  * full volume; d_workspace (>= fpgb_generate_workspace_size bytes, 256-byte
- * aligned) holds the per-voxel keys and the segment table, or NULL to use the
- * library's own cached device pool.  props/n_props/warnings are host memory;
+ * aligned) holds the segment and layer tables and the segment lists of the
+ * voxel bricks (the per-voxel winner keys stay in shared memory), or NULL to
+ * use the library's own cached device pool.  props/n_props/warnings are host memory;
  * warnings != NULL synchronises the stream. */
 size_t fpgb_generate_workspace_size(const fpgb_volume *vol,
                                     const fpgb_fibers *fibers);
@@ -121,8 +122,8 @@ int fpgb_generate_tissue_device(const fpgb_volume *vol,
  * fpgb_generate_tissue_device, but the scratch (segment and layer tables,
  * segment lists of the 8x8x32-voxel bricks) lives in a fixed 64 MiB
  * __device__ array of this library that every GPU loading it holds until
- * exit.  Problems needing more scratch (about 280 bytes per fiber segment
- * plus 4 per segment-brick overlap and 12 per brick: ~170,000 segments) are
+ * exit.  Problems needing more scratch (288 bytes per fiber segment plus 4
+ * per segment-brick overlap and 8 per brick: about 220,000 short segments) are
  * rejected with FPGB_EINVAL before any device work.  The first call on a device resolves the array's address with that
  * device current; make it before any stream capture.  All calls on a device
  * share the array: calls whose device work overlaps race and must be
@@ -251,7 +252,11 @@ int fpgb_rofl_device(const double *d_data, int64_t n_pix, int64_t n_rot, double 
                      const unsigned char *d_mask, double *d_out, int64_t *n_unconverged,
                      void *stream);
 
-/* Release the library's cached device pool on the current device. */
+/* Release the library's cached device pool on the current device.  The pool
+ * keeps device buffers per (stream, calling host thread) between calls of the
+ * host-buffer entry points and of device entry points given no workspace;
+ * this frees all of them (after synchronising the device), so it must not
+ * run while another thread is inside a call of this library. */
 int fpgb_release_pool(void);
 
 #ifdef __cplusplus

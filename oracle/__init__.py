@@ -27,7 +27,15 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_LIB = os.path.join(_HERE, "_lib", "liboracle.so")
 REF_LIB = os.path.join(_HERE, "_ref", "libpliref.so")
-REF_ROOT_DEFAULT = "/root/reference"
+# Checkout of the reference project (read only, never needed at run time on a
+# machine without it): FPGB_REFERENCE_ROOT, else the build container's path.
+REF_ROOT_DEFAULT = os.environ.get("FPGB_REFERENCE_ROOT", "/root/reference")
+
+
+def reference_file(*parts):
+    """Path of a file of the reference checkout, or None when it is absent."""
+    path = os.path.join(REF_ROOT_DEFAULT, *parts)
+    return path if os.path.exists(path) else None
 
 WARNING_NAMES = ("overlap", "single_point", "zero_axis", "not_normalized",
                  "empty_light", "layer_overflow")

@@ -21,7 +21,7 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
 from fastpli_gb300 import h5read  # noqa: E402
 
-REF_ROOT = "/root/reference"
+REF_ROOT = os.environ.get("FPGB_REFERENCE_ROOT", "/root/reference")
 
 
 def main():

@@ -21,7 +21,6 @@ import cases
 from fastpli_gb300 import analysis, io, objects
 from fastpli_gb300.simpli import Simpli
 
-REF_CUBE = "/root/reference/tests/cube.dat"
 
 
 def test_dat_round_trip(tmp_path):
@@ -48,9 +47,11 @@ def test_dat_blank_line_rules():
 
 
 def test_reference_cube_dat_matches_fixture():
-    if not os.path.exists(REF_CUBE):
-        pytest.skip("reference tree not present")
-    fbs = io.load(REF_CUBE)
+    import oracle
+    path = oracle.reference_file("tests", "cube.dat")
+    if path is None:
+        pytest.skip("reference checkout not present (set FPGB_REFERENCE_ROOT)")
+    fbs = io.load(path)
     ref = cases.load_cube()
     assert len(fbs) == 1 and len(list(fbs)[0]) == len(ref[0])
     for a, b in zip(list(fbs)[0], ref[0]):

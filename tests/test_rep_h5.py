@@ -26,7 +26,6 @@ import pytest
 import cases
 
 H5 = os.path.join(cases.GOLDEN, "simpli_rep_h5.npz")
-REF_H5 = "/root/reference/tests/simulation/simpli_rep.h5"
 TILTS_DEG = [(0, 0), (5.5, 0), (5.5, 90), (5.5, 180), (5.5, 270)]
 LAYERS = [(0.333, -0.004, 10, "p"), (0.666, 0, 5, "b"), (1.0, 0.004, 1, "r")]
 ROT6 = np.deg2rad([0, 30, 60, 90, 120, 150])
@@ -49,10 +48,12 @@ def angdist_deg(a, b, period=180.0):
 def test_fixture_is_the_reference_file():
     """The committed fixture holds exactly the reference file's datasets
     (checked where the reference tree is present)."""
-    if not os.path.exists(REF_H5):
-        pytest.skip("reference tree not present")
+    import oracle
+    path = oracle.reference_file("tests", "simulation", "simpli_rep.h5")
+    if path is None:
+        pytest.skip("reference checkout not present (set FPGB_REFERENCE_ROOT)")
     from fastpli_gb300 import h5read
-    data = h5read.read_all(REF_H5)
+    data = h5read.read_all(path)
     g = h5()
     assert sorted(k.replace("/", ".") for k in data) == sorted(g.files)
     for k, v in data.items():
