@@ -1,19 +1,44 @@
-"""Benchmark of the forward model on the crossing-bundle workload.
+"""Benchmark of the forward model.
 
-One step = the forward model of one volume: voxelize 2 x 1000 fibers of 50
-points into a 512x512x120 volume at 0.2 µm (generate_tissue) and march it at
-5 tilts ((0,0) and 5.5° at phi = 0/90/180/270°) x 9 polarizer angles with
-Slerp interpolation (run_simulation), epa fused.  Synthetic seeded fibers
-(``fastpli_gb300.synth.crossing``); the label + vector volume (503 MB) is
-larger than L2, so no flush is needed between steps.
+Default workload (the headline line): the uneven-tile batch — 256 independent
+tissue tiles, xy sides uniform 64-512 voxels, z 30-120 voxels at 0.2 µm, 50-2000
+fibers of uniformly random direction per tile with the tile's own dn in
+[-0.004, 0.004] and mu in [0, 20] (``fastpli_gb300.synth.tiles``, seeds
+1000 + i), each tile voxelized and marched at 5 tilts ((0,0) and 5.5° at
+phi = 0/90/180/270°) x 9 polarizer angles with Slerp interpolation.  One step
+= the whole batch (voxelize every tile + march every (tile, tilt) pair) as one
+CUDA-graph replay.  The 26 GB of label + vector fields are far larger than
+L2, so no flush is needed between steps.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+                    [--workload tiles|crossing|serve]
 
-Prints one JSON line (rank 0).  ``value`` is ray-voxel steps per second of
-the whole step, device-resident; ``e2e`` the same metric through the
-drop-in host API (host numpy in and out, copies inside the timed region).
-``--impl reference`` times the CPU forward model (the oracle's C
-restatement of the reference, all host threads) on the same workload.
+Prints one JSON line (rank 0):
+  value       ray-voxel steps/s of the batch, device-resident (fiber tables
+              already in HBM; CUDA-graph replays timed with CUDA events);
+  e2e         the same metric through the batch's C ABI with HOST buffers:
+              host planning from the flat fiber arrays, upload of the tables,
+              the batch, and one device-to-host copy of every image into
+              page-locked memory, per step (wall clock);
+  plain_per_call / e2e_plain_host_api
+              the same tiles through the plain per-call path (one voxelizer
+              call + 5 march calls per tile), device-resident and through the
+              drop-in host API (numpy label/vector out of run_generation and
+              back into each run_simulation, as Simpli does);
+  roofline    the dominant kernel (voxelizer or march, timed stage by stage)
+              against the measured HBM copy rate;
+  cpu_baseline / parity
+              the oracle (the C restatement of the reference, all host
+              threads) on a bounded sample of the same tiles, and the GPU
+              results of those tiles compared with it;
+  crossing / watson / serving
+              the 512x512x120 crossing-bundle volume (5 tilts), the
+              1024x1024x240 voxelization-heavy Watson volume (1 tilt) and a
+              short Poisson serving sweep (batched vs plain, p50/p99).
+
+``--impl reference`` times the CPU forward model (the oracle's C restatement
+of the reference, all host threads) on rotating samples of the same tiles; it
+loads nothing of this package's native library.
 """
 
 import argparse
@@ -30,8 +55,13 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "ray-voxel steps/s (forward model: voxelize + 5 tilts x 9 angles, Slerp)"
+METRIC = "ray-voxel steps/s (uneven tile batch: voxelize + 5 tilts x 9 angles, Slerp)"
 UNIT = "steps/s"
+N_TILES = 256
+CPU_SAMPLE_STRIDE = 8      # GPU arm's CPU baseline / parity: every 8th tile (32 tiles)
+REF_TILES_PER_STEP = 8     # reference arm: 8 consecutive tiles per step, rotating
+VOXELIZER_LAUNCHES = 4     # brick_bin (count), brick_scan, brick_bin (fill), voxel_bricks
+MARCH_LAUNCHES = 2         # batch_march untilted, tilted
 
 
 def _dist_env():
@@ -39,12 +69,6 @@ def _dist_env():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return ws, rank, local
-
-
-def _workload(rank=0):
-    from fastpli_gb300 import synth
-    # every rank voxelizes and marches its own seeded volume (weak scaling)
-    return synth.crossing(seed=2 + rank)
 
 
 class ClockSampler:
@@ -112,9 +136,9 @@ def _peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
             p = json.load(f)
-        return float(p["hbm_gbs"]), "measured"
+        return float(p["hbm_gbs"]), "measured", float(p.get("sm_max_mhz", 2070.0))
     except Exception:
-        return 6800.0, "fallback"
+        return 6800.0, "fallback", 2070.0
 
 
 def _ncu_metric(summary, name):
@@ -143,95 +167,46 @@ def _ncu_traffic(summary):
 
 
 def _ncu_limiter(summary):
-    """What bounds a kernel that is not HBM-bound, from the same summary:
-    the fraction of cycles the schedulers issued and the FMA-pipe load."""
+    """What bounds a kernel that is not HBM-bound, from the same summary."""
     issue = _ncu_metric(summary, "smsp__issue_active.avg.pct_of_peak_sustained_active")
-    fma = _ncu_metric(summary, "sm__pipe_fma_cycles_active.avg.pct_of_peak_sustained_active")
     if issue is None:
         return None
-    return {"kind": "instruction issue / latency (ncu)", "issue_active_frac": issue[0] / 100,
-            "fma_pipe_frac": None if fma is None else fma[0] / 100}
+    out = {"kind": "instruction issue / latency (ncu)", "issue_active_frac": issue[0] / 100,
+           "source": "profiles/" + summary}
+    dram = _ncu_metric(summary, "gpu__dram_throughput.avg.pct_of_peak_sustained_elapsed")
+    if dram is not None:
+        out["dram_frac"] = dram[0] / 100
+    return out
 
 
-# Per-step operation counts of the reference formulas for the march's
-# FP32 / SFU roofs (ray-voxel step with rho collapsed; background steps cost
-# one multiply): NN 50 FP32 + 4 SFU (sqrt, rcp, sin, cos); Slerp adds the 8
-# neighbour label compares and 7 interpolations of ~30 FP32 + acos + 2 sin +
-# rcp.  A vertical ray's interpolation collapses, so untilted steps count as NN.
-OPS_NN = (50, 4)
-OPS_SLERP = (50 + 8 + 7 * 30, 4 + 7 * 4)
-# voxelizer: one candidate test (a voxel of a segment's clipped box) is ~25
-# FP64 operations and one FP64 division in the reference
-FP64_PER_CANDIDATE = 26
+# Minimal thread instructions of one voxelizer candidate test (a voxel of a
+# segment's clipped box): the FP32 estimate of its distance to the segment
+# (about 10 FMAs: w = c - p, c1 = w.v, t = clamp(c1 / c2), |w - t v|^2),
+# the threshold compare and one shared-memory atomicMin of the winner key:
+# 16.  The issue roof is the GPU's thread-instruction rate over that count.
+VOXEL_MIN_INST = 16
 
 
-def measure_peaks():
-    """FP32 flop/s, SFU op/s, FP64 flop/s and L2 atomics/s of this GPU from the
-    microbenchmarks in fastpli_gb300/csrc/peaks (None if unavailable)."""
-    import ctypes
-    from fastpli_gb300 import build as fb
-    try:
-        lib = ctypes.CDLL(fb.PEAKS_LIB)
-    except OSError:
-        return None
-    lib.fpgb_measure_peaks.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
-    out = (ctypes.c_double * 4)()
-    if lib.fpgb_measure_peaks(out, None) != 0:
-        return None
-    return {"fp32_flops": out[0], "sfu_ops": out[1], "fp64_flops": out[2],
-            "l2_atomics": out[3]}
-
-
-def candidate_tests(w):
+def candidate_tests(tiles):
     """Voxels of every segment's clipped box (generator.cpp:295-312), the
-    voxelizer's algorithmic unit, from the fiber table on the host."""
-    X, Y, Z = (int(v) for v in w.dim)
+    voxelizer's algorithmic unit, from the fiber tables on the host."""
     total = 0
-    for fibers, layers in zip(w.bundles, w.layers):
-        smax = np.sqrt(max(l[0] for l in layers) ** 2)
-        for f in fibers:
-            p = (np.asarray(f[:, :3], np.float64) - np.asarray(w.origin)) * (1.0 / w.voxel_size)
-            r = np.asarray(f[:, 3], np.float64) * (1.0 / w.voxel_size)
-            rmax = np.maximum(r[:-1], r[1:]) * smax
-            lo = np.minimum(p[:-1], p[1:]) - rmax[:, None]
-            hi = np.maximum(p[:-1], p[1:]) + rmax[:, None]
-            lo = np.clip(lo, 0, [X, Y, Z])
-            hi = np.clip(hi, 0, [X, Y, Z])
-            ext = np.maximum(np.floor(hi + 0.5) - np.trunc(lo), 0)
-            total += int(np.prod(ext, axis=1).sum())
+    for w in tiles:
+        X, Y, Z = (int(v) for v in w.dim)
+        for fibers, layers in zip(w.bundles, w.layers):
+            smax = np.sqrt(max(l[0] for l in layers) ** 2)
+            if not len(fibers):
+                continue
+            pts = [np.asarray(f, np.float64) for f in fibers if len(f) > 1]
+            for f in pts:
+                p = (f[:, :3] - np.asarray(w.origin)) * (1.0 / w.voxel_size)
+                r = f[:, 3] * (1.0 / w.voxel_size)
+                rmax = np.maximum(r[:-1], r[1:]) * smax
+                lo = np.clip(np.minimum(p[:-1], p[1:]) - rmax[:, None], 0, [X, Y, Z])
+                hi = np.clip(np.maximum(p[:-1], p[1:]) + rmax[:, None], 0, [X, Y, Z])
+                ext = np.maximum(np.floor(hi + 0.5) - np.trunc(lo), 0)
+                total += int(np.prod(ext, axis=1).sum())
     return total
-
-
-def roofline_model(peaks, hbm_gbs, w, n_steps_untilted, n_steps_tilted, tissue_frac,
-                   march_steps_per_s, candidates, voxelize_s):
-    """The march against min(HBM, FP32, SFU) steps/s and the voxelizer against
-    the FP64 rate at the reference's per-candidate work."""
-    if peaks is None:
-        return None
-    f = tissue_frac
-    fp32 = ((f * OPS_NN[0] + 1 - f) * n_steps_untilted +
-            (f * OPS_SLERP[0] + 1 - f) * n_steps_tilted) / (n_steps_untilted + n_steps_tilted)
-    sfu = (f * OPS_NN[1] * n_steps_untilted + f * OPS_SLERP[1] * n_steps_tilted) / (
-        n_steps_untilted + n_steps_tilted)
-    roofs = {"hbm": hbm_gbs * 1e9 / 16, "fp32": peaks["fp32_flops"] / fp32,
-             "sfu": peaks["sfu_ops"] / sfu}
-    bound = min(roofs, key=roofs.get)
-    vox_roof = peaks["fp64_flops"] / FP64_PER_CANDIDATE
-    vox_rate = candidates / voxelize_s
-    return {
-        "measured_peaks": peaks,
-        "march": {"unit": "ray-voxel steps/s", "achieved": march_steps_per_s,
-                  "roofs": roofs, "bound": bound, "frac": march_steps_per_s / roofs[bound],
-                  "ops_per_step": {"fp32": fp32, "sfu": sfu}, "tissue_step_frac": f},
-        "voxelizer": {"unit": "candidate tests/s", "achieved": vox_rate,
-                      "candidates": candidates, "roof_fp64": vox_roof, "bound": "fp64",
-                      "frac": vox_rate / vox_roof},
-    }
-
-
-# kernels of one device-resident step: the voxelizer's segment binning (count,
-# scan, fill) and brick kernel, then one march per tilt
-VOXELIZER_LAUNCHES = 4
 
 
 def _setup_args(w):
@@ -241,51 +216,68 @@ def _setup_args(w):
             kw["flip_z"], kw["filter_rotations"])
 
 
+def _simulator(w):
+    from fastpli_gb300.simulation import _Simulator
+    sim = _Simulator()
+    sim.set_pli_setup(*_setup_args(w))
+    return sim
+
+
 # ---------------------------------------------------------------- CPU arm ---
-def cpu_forward(w, n_threads, tilts=None):
-    """The oracle's C restatement of the reference forward model; returns
-    (seconds, ray-voxel steps)."""
+def cpu_forward(tiles, n_threads, keep=False):
+    """The oracle's C restatement of the reference forward model over
+    ``tiles`` (voxelize, then every tilt); returns (seconds, ray-voxel steps,
+    outputs).  Steps are counted on the host with the reference's z loop
+    (oracle.count_steps), so nothing of the product library is loaded."""
     import oracle
-    oracle.build(ref=False)
-    from fastpli_gb300 import _native as N
-    tilts = w.tilts if tilts is None else tilts
     t0 = time.perf_counter()
-    lab, vec, props, _ = oracle.generate(w.dim, w.origin, w.voxel_size, w.bundles, w.layers,
-                                         n_threads=n_threads)
-    for theta, phi in tilts:
-        oracle.simulate(lab, vec, props, theta, phi, n_threads=n_threads, **w.setup_kwargs())
-    dt = time.perf_counter() - t0
-    s = N.SetupBlock(*_setup_args(w))
-    d = np.asarray(w.dim, np.int64)
-    steps = sum(int(N.load(build_if_missing=False).fpgb_count_steps(
-        N.byref(s.struct), N.ptr(d), float(t), float(p))) for t, p in tilts)
-    return dt, steps
+    steps, outs = 0, []
+    for w in tiles:
+        lab, vec, props, _ = oracle.generate(w.dim, w.origin, w.voxel_size, w.bundles, w.layers,
+                                             n_threads=n_threads)
+        imgs = [oracle.simulate(lab, vec, props, th, ph, n_threads=n_threads,
+                                **w.setup_kwargs())[0] for th, ph in w.tilts]
+        steps += sum(oracle.count_steps(w.dim, th, w.setup_kwargs()["step_size"])
+                     for th, _ in w.tilts)
+        if keep:
+            outs.append((lab, vec, imgs))
+    return time.perf_counter() - t0, steps, outs
 
 
 def run_reference(args):
     ws, rank, _ = _dist_env()
     if rank != 0:
         return 0
-    w = _workload(0)
-    from fastpli_gb300 import build as nb
-    nb.build()
+    import oracle
+    from fastpli_gb300 import synth
+    oracle.build(ref=False)
     threads = os.cpu_count() or 1
-    for _ in range(max(0, min(args.warmup, 1))):
-        cpu_forward(w, threads, tilts=w.tilts[:1])
-    times, steps = [], 0
-    for _ in range(args.steps):
-        dt, steps = cpu_forward(w, threads)
+    k = REF_TILES_PER_STEP
+
+    def sample(step):
+        return [synth.tile((step * k + j) % N_TILES) for j in range(k)]
+
+    for i in range(min(args.warmup, 2)):
+        cpu_forward(sample(N_TILES // k - 1 - i), threads)
+    times, steps = [], []
+    for i in range(args.steps):
+        tiles = sample(i)  # generating the fibers is not timed
+        dt, st, _ = cpu_forward(tiles, threads)
         times.append(dt)
-    value = steps / (sum(times) / len(times))
+        steps.append(st)
+    value = sum(steps) / sum(times)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
-            "config": dict(w.describe(), inputs="fibers (host)",
-                           parallelism=f"OpenMP {threads} threads"),
+            "config": {"workload": f"uneven tile batch, {N_TILES} tiles (xy 64-512, z 30-120 "
+                                   f"@ 0.2 um, 50-2000 fibers, 5 tilts x 9 angles, Slerp)",
+                       "inputs": "fibers (host)", "parallelism": f"OpenMP {threads} threads"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": "full forward-model steps of the workload"},
+                             "sample": f"{k} consecutive tiles of the {N_TILES}-tile mixture "
+                                       f"per step, rotating ({args.steps * k} tiles timed); "
+                                       "voxelize + 5 tilts each"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -293,7 +285,52 @@ def run_reference(args):
 
 
 # ---------------------------------------------------------------- GPU arm ---
+def _events(n):
+    import torch
+    return [torch.cuda.Event(enable_timing=True) for _ in range(n)]
+
+
+def measure_stages(b, reps, stream):
+    """Voxelizer and march of the batch timed separately (CUDA events on the
+    launching stream): average ms of each."""
+    import torch
+    ev = [_events(3) for _ in range(reps)]
+    with torch.cuda.stream(stream):
+        for e in ev:
+            e[0].record(stream)
+            b.run(stages=1, stream=stream)
+            e[1].record(stream)
+            b.run(stages=2, stream=stream)
+            e[2].record(stream)
+    torch.cuda.synchronize()
+    vox = sum(e[0].elapsed_time(e[1]) for e in ev) / reps
+    march = sum(e[1].elapsed_time(e[2]) for e in ev) / reps
+    return vox, march
+
+
+def plain_device_pass(tiles, sim, bufs):
+    """The plain per-call path over the tiles, device-resident: one
+    voxelizer call and 5 march calls per tile."""
+    for (g, t, lab, vec, img, wsp) in bufs:
+        _, _, props, _ = g.run_generation_device(label=lab, vector=vec, workspace=wsp,
+                                                 sync_warnings=False)
+        for th, ph in t.tilts:
+            sim.run_simulation_device(t.dim, lab, vec, props, float(th), float(ph), image=img,
+                                      sync_warnings=False)
+
+
+def plain_host_pass(tiles, sim, gens):
+    """The drop-in host API over the tiles, as Simpli drives it: numpy label /
+    vector fields out of run_generation, passed back into run_simulation for
+    every tilt; images returned as numpy."""
+    for g, t in zip(gens, tiles):
+        lab, vec, props = g.run_generation()
+        for th, ph in t.tilts:
+            sim.run_simulation(t.dim, lab, vec, props, float(th), float(ph))
+
+
 def run_gpu(args):
+    import warnings as _w
     import torch
     ws, rank, local = _dist_env()
     torch.cuda.set_device(local)
@@ -301,161 +338,216 @@ def run_gpu(args):
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    from fastpli_gb300.simulation import _Generator, _Simulator
     import fastpli_gb300
+    from fastpli_gb300 import autotune, synth
+    from fastpli_gb300 import batch as B
+    from fastpli_gb300.shard import rank_units
+    from fastpli_gb300.simulation import _Generator
     fastpli_gb300.native_library()
-
-    w = _workload(rank)
-    X, Y, Z = (int(v) for v in w.dim)
-    g = _Generator()
-    g.set_volume(w.dim, w.origin, w.voxel_size)
-    g.set_fiber_bundles(w.bundles, w.layers)
-    sim = _Simulator()
-    sim.set_pli_setup(*_setup_args(w))
-    steps_per = sum(sim.count_steps(w.dim, float(t), float(p)) for t, p in w.tilts)
-    n_rho = sim.n_rho
+    _w.simplefilter("ignore")  # "objects overlap" etc.: the tiles overlap by design
     dev = torch.device("cuda", local)
-    label = torch.empty((X, Y, Z), dtype=torch.int32, device=dev)
-    vector = torch.empty((X, Y, Z, 3), dtype=torch.float32, device=dev)
-    images = [torch.empty((X, Y, n_rho), dtype=torch.float64, device=dev) for _ in w.tilts]
-    wsp = torch.empty(g.workspace_size(), dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream()
-    _, _, props, _ = g.run_generation_device(label=label, vector=vector, workspace=wsp)
-    tissue_voxels = int((label > 0).sum().item())
 
-    def step(ev=None):
-        if ev:
-            ev[0].record(stream)
-        g.run_generation_device(label=label, vector=vector, workspace=wsp,
-                                sync_warnings=False)
-        if ev:
-            ev[1].record(stream)
-        sim.run_tilts_device(w.dim, label, vector, props, w.tilts, images=images,
-                             sync_warnings=False)
-        if ev:
-            ev[2].record(stream)
-
+    all_params = [synth.tile_params(i) for i in range(N_TILES)]
+    mine = rank_units([int(np.prod(p[0])) for p in all_params], ws, rank)
+    tiles = [synth.tile(i) for i in mine]
+    kw = tiles[0].setup_kwargs()
+    flats = B.flatten(tiles)
+    b = B.TileBatch(tiles, kw, flat_fibers=flats).allocate()
+    cfg, _, _ = autotune.tune(b, reps=1)
+    b.capture()
+    steps = b.steps
+    n_pairs = int(b.info.n_pairs)
     for _ in range(args.warmup):
-        step()
+        b.replay()
     torch.cuda.synchronize()
-    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
-        t0 = torch.cuda.Event(enable_timing=True)
-        t1 = torch.cuda.Event(enable_timing=True)
-        t0.record(stream)
-        for i in range(args.steps):
-            step(evs[i])
-        t1.record(stream)
+        e0, e1 = _events(2)
+        e0.record(stream)
+        for _ in range(args.steps):
+            b.replay()
+        e1.record(stream)
         torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    ms_total = t0.elapsed_time(t1)
-    gen_ms = [e[0].elapsed_time(e[1]) for e in evs]
-    march_ms = [e[1].elapsed_time(e[2]) for e in evs]
+    ms_step = e0.elapsed_time(e1) / args.steps
     if dist:
-        tt = torch.tensor([ms_total], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms_total = float(tt.item())
-    ms_step = ms_total / args.steps
-    value = ws * steps_per / (ms_step * 1e-3)
+        from fastpli_gb300.shard import max_over_ranks
+        ms_step = max_over_ranks(ms_step, dist, device=dev)
+    value = ws * steps / (ms_step * 1e-3)
 
-    # ----- e2e through the drop-in host API (numpy in/out) ---------------
-    # three full untimed steps first: the first host-API steps after the
-    # device loop pay one-off costs (pool growth, page-locked host blocks)
-    e2e_steps = max(3, min(args.steps, 10))
-    # (the warm-up steps keep their results alive exactly as the timed steps
-    # do, so the host allocator's cache holds the blocks the timed loop needs)
-    for _ in range(3):
-        lab_h, vec_h, props_h = g.run_generation()
-        imgs = [sim.run_simulation(w.dim, lab_h, vec_h, props_h, float(t), float(p))
-                for t, p in w.tilts]
+    # ----- stage split (voxelizer | march), for the roofline --------------
+    vox_ms, march_ms = measure_stages(b, 3, stream)
+
+    # ----- parity sample: GPU results of the CPU-baseline tiles -----------
+    b.replay()
+    torch.cuda.synchronize()
+    sample_idx = list(range(0, len(tiles), CPU_SAMPLE_STRIDE))
+    gpu_sample = [(b.label(t).cpu().numpy(), b.vector(t).cpu().numpy(),
+                   [b.image(p).cpu().numpy() for p in b.pairs_of(t)]) for t in sample_idx]
+
+    # ----- e2e through the batch C ABI with host buffers --------------------
+    host_out = torch.empty(b.output_bytes, dtype=torch.uint8, pin_memory=True)
+    arena, wsp = b.arena, b.workspace
+
+    def e2e_step():
+        bb = B.TileBatch(tiles, kw, flat_fibers=flats)
+        bb.allocate(arena=arena, workspace=wsp)
+        bb.config = cfg
+        bb.run()
+        bb.outputs_host(out=host_out)
+        return bb
+
+    e2e_n = max(3, min(args.steps, 10))
+    for _ in range(2):
+        last = e2e_step()
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    e2e_step_s = []
-    for _ in range(e2e_steps):
-        t_e2e = time.perf_counter()
-        lab_h, vec_h, props_h = g.run_generation()
-        imgs = [sim.run_simulation(w.dim, lab_h, vec_h, props_h, float(t), float(p))
-                for t, p in w.tilts]
-        e2e_step_s.append(time.perf_counter() - t_e2e)
-    e2e_s = sum(e2e_step_s) / e2e_steps
+    e2e_s = []
+    for _ in range(e2e_n):
+        t0 = time.perf_counter()
+        last = e2e_step()
+        e2e_s.append(time.perf_counter() - t0)
+    e2e_mean = sum(e2e_s) / len(e2e_s)
     if dist:
-        tt = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_s = float(tt.item())
-    vol_bytes = X * Y * Z * 16
-    img_bytes = X * Y * n_rho * 8
-    fib_bytes = int(sum(f.nbytes for b in w.bundles for f in b))
-    h2d = fib_bytes + len(w.tilts) * vol_bytes
-    d2h = vol_bytes + len(w.tilts) * img_bytes
-    del imgs
+        from fastpli_gb300.shard import max_over_ranks
+        e2e_mean = max_over_ranks(e2e_mean, dist, device=dev)
+    h2d, d2h = last.upload_bytes, last.output_bytes
+    last.close()
+    b.close()  # the graph and the handle
+    del last, arena, wsp, host_out
+    b = None
+    torch.cuda.empty_cache()
 
-    # ----- roofline of the dominant kernel ------------------------------
-    hbm_peak, peak_kind = _peaks()
-    gen_avg = sum(gen_ms) / len(gen_ms)
-    march_avg = sum(march_ms) / len(march_ms)
-    n_untilted = sum(sim.count_steps(w.dim, float(t), float(p))
-                     for t, p in w.tilts if float(t) == 0.0)
-    model = roofline_model(measure_peaks(), hbm_peak, w, n_untilted, steps_per - n_untilted,
-                           tissue_voxels / float(X * Y * Z), steps_per / (march_avg * 1e-3),
-                           candidate_tests(w), gen_avg * 1e-3)
-    # march: one label (4 B) and one axis (12 B) per ray-voxel step
-    march_bytes = 16 * steps_per
-    march_gbs = march_bytes / (march_avg * 1e-3) / 1e9
-    # voxelizer: label + vector written once per voxel (16 B); the winner keys
-    # stay in shared memory, the segment table (280 B per segment) is noise
-    gen_bytes = 16 * X * Y * Z
-    gen_gbs = gen_bytes / (gen_avg * 1e-3) / 1e9
-    if march_avg >= gen_avg:
-        prof = "march_rays_slerp_tilted_crossing512x512x120.md"
-        traffic = _ncu_traffic(prof)
-        roof = {"kernel": "march_rays (5 tilts)", "bound": "hbm", "achieved": march_gbs,
-                "peak": hbm_peak, "unit": "GB/s", "frac": march_gbs / hbm_peak,
-                "traffic": traffic, "traffic_per": "one tilted launch (ncu)",
-                "limiter": _ncu_limiter(prof),
-                "algorithmic_bytes_per_launch": march_bytes / len(w.tilts),
+    # ----- the plain per-call path on the same tiles ------------------------
+    sim = _simulator(tiles[0])
+    gens, bufs = [], []
+    for t in tiles:
+        g = _Generator()
+        g.set_volume(t.dim, t.origin, t.voxel_size)
+        g.set_fiber_bundles(t.bundles, t.layers)
+        gens.append(g)
+    for g, t in zip(gens, tiles):
+        X, Y, Z = (int(v) for v in t.dim)
+        bufs.append((g, t, torch.empty((X, Y, Z), dtype=torch.int32, device=dev),
+                     torch.empty((X, Y, Z, 3), dtype=torch.float32, device=dev),
+                     torch.empty((X, Y, sim.n_rho), dtype=torch.float64, device=dev),
+                     torch.empty(g.workspace_size(), dtype=torch.uint8, device=dev)))
+    plain_device_pass(tiles, sim, bufs)
+    torch.cuda.synchronize()
+    p0, p1 = _events(2)
+    p0.record(stream)
+    plain_device_pass(tiles, sim, bufs)
+    p1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = p0.elapsed_time(p1)
+    del bufs
+    torch.cuda.empty_cache()
+    plain_host_pass(tiles[:8], sim, gens[:8])  # warm the host allocator
+    t0 = time.perf_counter()
+    plain_host_pass(tiles, sim, gens)
+    plain_host_s = time.perf_counter() - t0
+    vol_bytes = sum(int(np.prod(t.dim)) * 16 for t in tiles)
+    img_bytes = sum(int(t.dim[0] * t.dim[1]) * sim.n_rho * 8 * len(t.tilts) for t in tiles)
+    fib_bytes = sum(f.nbytes for t in tiles for bnd in t.bundles for f in bnd)
+    plain_h2d = fib_bytes + sum(int(np.prod(t.dim)) * 16 * len(t.tilts) for t in tiles)
+
+    # ----- roofline of the dominant kernel ----------------------------------
+    hbm, peak_kind, sm_mhz = _peaks()
+    vox = sum(int(np.prod(t.dim)) for t in tiles)
+    march_bytes = 16 * steps
+    vox_bytes = 16 * vox
+    march_gbs = march_bytes / (march_ms * 1e-3) / 1e9
+    vox_gbs = vox_bytes / (vox_ms * 1e-3) / 1e9
+    if march_ms >= vox_ms:
+        prof = "batch_march_tiles256.md"
+        roof = {"kernel": "batch_march (2 launches: untilted, tilted)", "bound": "hbm",
+                "achieved": march_gbs, "peak": hbm, "unit": "GB/s", "frac": march_gbs / hbm,
+                "traffic": _ncu_traffic(prof), "traffic_per": "batch (ncu)",
+                "limiter": _ncu_limiter(prof), "algorithmic_bytes_per_launch": march_bytes,
                 "algorithmic_bytes_per_step": 16, "peak_source": peak_kind}
     else:
-        prof = "voxel_bricks_crossing512x512x120.md"
-        traffic = _ncu_traffic(prof)
-        roof = {"kernel": "voxel_bricks (+ binning)", "bound": "hbm", "achieved": gen_gbs,
-                "peak": hbm_peak, "unit": "GB/s", "frac": gen_gbs / hbm_peak,
-                "traffic": traffic, "traffic_per": "one launch (ncu)",
-                "limiter": _ncu_limiter(prof),
-                "algorithmic_bytes_per_launch": gen_bytes,
+        prof = "voxel_bricks_tiles256.md"
+        roof = {"kernel": "voxel_bricks (+ binning)", "bound": "hbm", "achieved": vox_gbs,
+                "peak": hbm, "unit": "GB/s", "frac": vox_gbs / hbm,
+                "traffic": _ncu_traffic(prof), "traffic_per": "one launch (ncu)",
+                "limiter": _ncu_limiter(prof), "algorithmic_bytes_per_launch": vox_bytes,
                 "algorithmic_bytes_per_voxel": 16, "peak_source": peak_kind}
+    cands = candidate_tests(tiles)
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    issue_rate = sms * 4 * 32 * sm_mhz * 1e6  # thread instructions per second
+    hbm_steps = hbm * 1e9 / 16
+    model = {
+        "march": {"unit": "ray-voxel steps/s", "achieved": steps / (march_ms * 1e-3),
+                  "roof_hbm": hbm_steps, "frac_hbm": steps / (march_ms * 1e-3) / hbm_steps,
+                  "ms": march_ms, "bytes_per_step": 16},
+        "voxelizer": {"unit": "candidate tests/s", "candidates": cands,
+                      "achieved": cands / (vox_ms * 1e-3), "ms": vox_ms,
+                      "roof_issue": issue_rate / VOXEL_MIN_INST,
+                      "frac_issue": cands / (vox_ms * 1e-3) / (issue_rate / VOXEL_MIN_INST),
+                      "min_thread_inst_per_candidate": VOXEL_MIN_INST,
+                      "frac_hbm": vox_gbs / hbm, "bytes_per_voxel": 16},
+        "batch": {"unit": "ray-voxel steps/s", "achieved": steps / (ms_step * 1e-3),
+                  "roof_hbm": hbm_steps, "frac_hbm": steps / (ms_step * 1e-3) / hbm_steps,
+                  "target_frac": 0.6,
+                  "note": "voxelizer + march of the batch against the march's HBM roof "
+                          "(16 B per ray-voxel step)"},
+    }
 
     line = None
     if rank == 0:
-        cpu = None
+        cpu, par = None, None
         if ws == 1 and not args.no_cpu:
+            import oracle
+            oracle.build(ref=False)
             threads = os.cpu_count() or 1
-            dt, st = cpu_forward(w, threads)
+            sample = [tiles[t] for t in sample_idx]
+            dt, st, outs = cpu_forward(sample, threads, keep=True)
             cpu = {"value": st / dt, "unit": UNIT, "cores": threads, "kind": "port",
-                   "sample": "one full forward-model step of the workload (oracle C "
-                             "restatement, OpenMP)"}
+                   "sample": f"{len(sample)} of the {len(tiles)} tiles (every "
+                             f"{CPU_SAMPLE_STRIDE}th), voxelize + 5 tilts each "
+                             "(oracle C restatement, OpenMP)"}
+            par = parity_of(gpu_sample, outs)
+        extra = {}
+        if not args.quick:
+            extra["crossing"] = measure_crossing(dev)
+            extra["watson"] = measure_watson(dev)
+            if args.serve_seconds > 0:
+                extra["serving"] = serve_sweep(args.rates, args.serve_seconds,
+                                               args.max_requests, 20, local, pool=tiles)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
-            "config": dict(w.describe(), l2="inputs larger than L2 (503 MB volume)",
-                           parallelism=f"replicas x{ws}"),
-            "tissue_voxels_per_s": tissue_voxels / (gen_avg * 1e-3),
-            "voxelize_ms": gen_avg, "march_ms": march_avg,
-            "march_steps_per_s": steps_per / (march_avg * 1e-3),
-            "roofline": roof, "roofline_model": model, "cpu_baseline": cpu,
-            "e2e": {"value": ws * steps_per / e2e_s, "unit": UNIT,
-                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "steps": e2e_steps, "step_ms_mean": 1e3 * e2e_s,
-                    "step_ms_min": 1e3 * min(e2e_step_s),
-                    "step_ms_max": 1e3 * max(e2e_step_s)},
-            "gpu_launches": args.steps * (VOXELIZER_LAUNCHES + len(w.tilts)),
+            "config": {"workload": f"uneven tile batch, {N_TILES} tiles (xy 64-512, z 30-120 "
+                                   f"@ 0.2 um, 50-2000 fibers, 5 tilts x 9 angles, Slerp)",
+                       "tiles": len(tiles), "voxels": vox, "pairs": n_pairs,
+                       "ray_voxel_steps": steps, "graph": "CUDA graph replay",
+                       "march_config": {"ctas_per_sm": cfg[0], "items_per_grab": cfg[1],
+                                        "coop": cfg[2]},
+                       "l2": f"inputs larger than L2 ({vox_bytes / 1e9:.1f} GB of fields)",
+                       "parallelism": f"replicas x{ws} (tiles sharded)"},
+            "tissue_voxels_per_s": vox / (vox_ms * 1e-3),
+            "voxelize_ms": vox_ms, "march_ms": march_ms,
+            "plain_per_call": {"ms_per_batch": plain_ms, "steps_per_s": steps / (plain_ms * 1e-3),
+                               "batched_speedup": plain_ms / ms_step},
+            "roofline": roof, "roofline_model": model, "cpu_baseline": cpu, "parity": par,
+            "e2e": {"value": ws * steps / e2e_mean, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "steps": e2e_n, "step_ms_mean": 1e3 * e2e_mean,
+                    "step_ms_min": 1e3 * min(e2e_s), "step_ms_max": 1e3 * max(e2e_s),
+                    "path": "fpgb_batch_create/upload/run + one D2H copy of all images"},
+            "e2e_plain_host_api": {"value": steps / plain_host_s, "unit": UNIT,
+                                   "ms_per_batch": 1e3 * plain_host_s,
+                                   "h2d_bytes_per_step": plain_h2d,
+                                   "d2h_bytes_per_step": vol_bytes + img_bytes},
+            "gpu_launches": args.steps * (VOXELIZER_LAUNCHES + MARCH_LAUNCHES),
             "clocks": clocks.summary(),
+            **extra,
         }
         print(json.dumps(line), flush=True)
     if dist:
@@ -463,118 +555,151 @@ def run_gpu(args):
     return 0
 
 
-# ----------------------------------------------------------- tiles mode ---
-def run_tiles(args):
-    """Batched uneven tiles (``--workload tiles``): N tiles of the uneven-tile
-    mixture (xy 64-512, z 30-120 voxels at 0.2 um, 50-2000 fibers, per-tile
-    dn/mu), 5 tilts x 9 angles each, Slerp.  One step = the whole batch
-    (voxelize all tiles + march all pairs) replayed from a CUDA graph; the
-    plain per-call path (per tile: voxelize, then one march per tilt) is timed
-    on the same tiles for comparison."""
+def parity_of(gpu, cpu):
+    """Label / vector mismatches and image errors of the GPU results against
+    the oracle's, over the sampled tiles."""
+    n_lab = n_vec = 0
+    rel = rel_mean = 0.0
+    pixels = 0
+    for (gl, gv, gi), (cl, cv, ci) in zip(gpu, cpu):
+        n_lab += int((gl != cl).sum())
+        n_vec += int((gv.view(np.uint32) != cv.view(np.uint32)).sum())
+        for a, r in zip(gi, ci):
+            rel = max(rel, float(np.max(np.abs(a - r) / np.maximum(np.abs(r), 1e-300))))
+            m = np.maximum(np.abs(r.mean(-1, keepdims=True)), 1e-300)
+            rel_mean = max(rel_mean, float(np.max(np.abs(a - r) / m)))
+            pixels += r.size
+    return {"against": "oracle (FP64 C restatement, pinned to the reference build)",
+            "tiles": len(gpu), "label_mismatches": n_lab, "vector_mismatches": n_vec,
+            "image_max_rel": rel, "image_max_rel_to_pixel_mean": rel_mean,
+            "image_values": pixels, "bars": {"labels": 0, "vectors": 0, "image_rel": 1e-4}}
+
+
+# ------------------------------------------------- the other workloads ---
+def measure_crossing(dev, steps=10, warmup=3):
+    """The 512x512x120 crossing-bundle volume: voxelize + 5 tilts per step,
+    device-resident, and through the drop-in host API."""
     import torch
-    from fastpli_gb300 import autotune, synth
-    from fastpli_gb300.batch import TileBatch
-    from fastpli_gb300.simulation import _Generator, _Simulator
-    import fastpli_gb300
-    ws, rank, local = _dist_env()
-    torch.cuda.set_device(local)
-    fastpli_gb300.native_library()
-    from fastpli_gb300.shard import rank_units
-    tiles_all = synth.tiles(args.tiles)
-    mine = rank_units([t.n_voxels for t in tiles_all], ws, rank)
-    tiles = [tiles_all[i] for i in mine]
-    kw = tiles[0].setup_kwargs()
-    b = TileBatch(tiles, kw).allocate()
-    cfg, _, _ = autotune.tune(b, reps=1)
-    b.capture()
-    for _ in range(args.warmup):
-        b.replay()
+    from fastpli_gb300 import synth
+    from fastpli_gb300.simulation import _Generator
+    w = synth.crossing(seed=2)
+    X, Y, Z = (int(v) for v in w.dim)
+    g = _Generator()
+    g.set_volume(w.dim, w.origin, w.voxel_size)
+    g.set_fiber_bundles(w.bundles, w.layers)
+    sim = _simulator(w)
+    n_steps = sum(sim.count_steps(w.dim, float(t), float(p)) for t, p in w.tilts)
+    label = torch.empty((X, Y, Z), dtype=torch.int32, device=dev)
+    vector = torch.empty((X, Y, Z, 3), dtype=torch.float32, device=dev)
+    images = [torch.empty((X, Y, sim.n_rho), dtype=torch.float64, device=dev) for _ in w.tilts]
+    wsp = torch.empty(g.workspace_size(), dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+    _, _, props, _ = g.run_generation_device(label=label, vector=vector, workspace=wsp)
+    tissue = int((label > 0).sum().item())
+    ev = [_events(3) for _ in range(steps)]
+
+    def step(e=None):
+        if e:
+            e[0].record(stream)
+        g.run_generation_device(label=label, vector=vector, workspace=wsp, sync_warnings=False)
+        if e:
+            e[1].record(stream)
+        sim.run_tilts_device(w.dim, label, vector, props, w.tilts, images=images,
+                             sync_warnings=False)
+        if e:
+            e[2].record(stream)
+
+    for _ in range(warmup):
+        step()
     torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clocks:
-        e0.record()
-        for _ in range(args.steps):
-            b.replay()
-        e1.record()
-        torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / args.steps
-    w = b.warnings()
-    steps = b.steps
-    vox = int(b.info.total_voxels)
-    # plain per-call path on the same tiles (device resident, no host copies)
-    sim = _Simulator()
-    sim.set_pli_setup(*_setup_args(tiles[0]))
-    gens = []
-    for t in tiles:
-        g = _Generator()
-        g.set_volume(t.dim, t.origin, t.voxel_size)
-        g.set_fiber_bundles(t.bundles, t.layers)
-        X, Y, Z = (int(v) for v in t.dim)
-        lab = torch.empty((X, Y, Z), dtype=torch.int32, device="cuda")
-        vec = torch.empty((X, Y, Z, 3), dtype=torch.float32, device="cuda")
-        img = torch.empty((X, Y, sim.n_rho), dtype=torch.float64, device="cuda")
-        wsp = torch.empty(g.workspace_size(), dtype=torch.uint8, device="cuda")
-        gens.append((g, t, lab, vec, img, wsp))
-
-    def plain():
-        for g, t, lab, vec, img, wsp in gens:
-            _, _, props, _ = g.run_generation_device(label=lab, vector=vec, workspace=wsp,
-                                                     sync_warnings=False)
-            for th, ph in t.tilts:
-                sim.run_simulation_device(t.dim, lab, vec, props, float(th), float(ph),
-                                          image=img, sync_warnings=False)
-    import warnings as _w
-    with _w.catch_warnings():
-        _w.simplefilter("ignore")
-        plain()
-        torch.cuda.synchronize()
-        p0 = time.perf_counter()
-        e0.record()
-        plain()
-        e1.record()
-        torch.cuda.synchronize()
-        plain_wall = time.perf_counter() - p0
-    plain_ms = e0.elapsed_time(e1)
-    ms = max_over_ranks_ms(ms, ws, local)
-    if rank == 0:
-        line = {"metric": "ray-voxel steps/s (uneven tile batch, voxelize + 5 tilts x 9 angles, "
-                          "Slerp)", "value": ws * steps / (ms * 1e-3), "unit": UNIT, "n_gpus": ws,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": "f32", "data": "synthetic",
-                "config": {"workload": f"{len(tiles)} uneven tiles (64-512 xy, 30-120 z)",
-                           "voxels": vox, "pairs": int(b.info.n_pairs),
-                           "graph": "CUDA graph replay", "march_config": list(cfg),
-                           "l2": "inputs larger than L2"},
-                "tissue_voxels_per_s": None,
-                "plain_per_call": {"ms_per_batch_device": plain_ms,
-                                   "ms_per_batch_wall": plain_wall * 1e3,
-                                   "steps_per_s": steps / (plain_ms * 1e-3)},
-                "fp64_replays": w["fp64_replays"], "clocks": clocks.summary()}
-        print(json.dumps(line), flush=True)
-    b.close()
-    return 0
+    t0, t1 = _events(2)
+    t0.record(stream)
+    for e in ev:
+        step(e)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    ms = t0.elapsed_time(t1) / steps
+    gen_ms = sum(e[0].elapsed_time(e[1]) for e in ev) / steps
+    march_ms = sum(e[1].elapsed_time(e[2]) for e in ev) / steps
+    for _ in range(3):
+        lab_h, vec_h, props_h = g.run_generation()
+        imgs = [sim.run_simulation(w.dim, lab_h, vec_h, props_h, float(t), float(p))
+                for t, p in w.tilts]
+    e2e = []
+    for _ in range(5):
+        t_e = time.perf_counter()
+        lab_h, vec_h, props_h = g.run_generation()
+        imgs = [sim.run_simulation(w.dim, lab_h, vec_h, props_h, float(t), float(p))
+                for t, p in w.tilts]
+        e2e.append(time.perf_counter() - t_e)
+    del imgs
+    hbm, _, _ = _peaks()
+    return {"workload": "crossing 512x512x120 @ 0.2 um, 2 x 1000 fibers, 5 tilts x 9 angles, "
+                        "Slerp",
+            "steps_per_s": n_steps / (ms * 1e-3), "ms_per_step": ms, "voxelize_ms": gen_ms,
+            "march_ms": march_ms, "tissue_voxels_per_s": tissue / (gen_ms * 1e-3),
+            "march_frac_hbm": 16 * n_steps / (march_ms * 1e-3) / (hbm * 1e9),
+            "e2e_host_api": {"steps_per_s": n_steps / (sum(e2e) / len(e2e)),
+                             "ms_per_step": 1e3 * sum(e2e) / len(e2e),
+                             "h2d_bytes_per_step": len(w.tilts) * X * Y * Z * 16,
+                             "d2h_bytes_per_step": X * Y * Z * 16 +
+                             len(w.tilts) * X * Y * sim.n_rho * 8}}
 
 
-# ----------------------------------------------------------- serve mode ---
-def run_serve(args):
-    """Serving (``--workload serve``): Poisson arrivals at each rate of
-    ``--rates``; every request is a tile of the uneven-tile mixture (a pool of
-    ``--pool`` seeded tiles) with 1 or 5 tilts (Bernoulli 1/2), Slerp, epa on
-    the device; HBM admission budget 150 GB.  The continuous-batching server
-    is compared with the plain per-call path serving the same arrival stream
-    one request at a time.  Reports p50/p99 arrival-to-result latency and
-    throughput per rate."""
+def measure_watson(dev, steps=3):
+    """The voxelization-heavy volume: 1024x1024x240 at 0.1 um, 20,000 fibers
+    of 50 points (Watson kappa = 5), 3 layers; voxelize + 1 tilt."""
     import torch
+    from fastpli_gb300 import synth
+    from fastpli_gb300.simulation import _Generator
+    w = synth.watson()
+    X, Y, Z = (int(v) for v in w.dim)
+    g = _Generator()
+    g.set_volume(w.dim, w.origin, w.voxel_size)
+    g.set_fiber_bundles(w.bundles, w.layers)
+    sim = _simulator(w)
+    label = torch.empty((X, Y, Z), dtype=torch.int32, device=dev)
+    vector = torch.empty((X, Y, Z, 3), dtype=torch.float32, device=dev)
+    image = torch.empty((X, Y, sim.n_rho), dtype=torch.float64, device=dev)
+    wsp = torch.empty(g.workspace_size(), dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+    _, _, props, _ = g.run_generation_device(label=label, vector=vector, workspace=wsp)
+    tissue = int((label > 0).sum().item())
+    n_steps = sim.count_steps(w.dim, 0.0, 0.0)
+    ev = [_events(3) for _ in range(steps)]
+    for e in [None] + ev:
+        if e:
+            e[0].record(stream)
+        g.run_generation_device(label=label, vector=vector, workspace=wsp, sync_warnings=False)
+        if e:
+            e[1].record(stream)
+        sim.run_simulation_device(w.dim, label, vector, props, 0.0, 0.0, image=image,
+                                  sync_warnings=False)
+        if e:
+            e[2].record(stream)
+    torch.cuda.synchronize()
+    gen_ms = sum(e[0].elapsed_time(e[1]) for e in ev) / steps
+    march_ms = sum(e[1].elapsed_time(e[2]) for e in ev) / steps
+    del label, vector, image, wsp
+    torch.cuda.empty_cache()
+    return {"workload": "watson 1024x1024x240 @ 0.1 um, 20000 fibers, 3 layers, 1 tilt",
+            "voxelize_ms": gen_ms, "march_ms": march_ms,
+            "tissue_voxels_per_s": tissue / (gen_ms * 1e-3), "voxels": X * Y * Z,
+            "steps_per_s": n_steps / (march_ms * 1e-3),
+            "forward_ms": gen_ms + march_ms}
+
+
+def serve_sweep(rates, seconds, max_requests, min_requests, local, pool_n=N_TILES, pool=None):
+    """Poisson arrivals at each rate; every request a tile of the uneven-tile
+    mixture with 1 or 5 tilts (Bernoulli 1/2), Slerp, epa on the device; the
+    continuous-batching server against the plain per-call path serving the
+    same stream one request at a time."""
     import warnings as _w
+    import torch
     from fastpli_gb300 import serving, synth
-    import fastpli_gb300
-    ws, rank, local = _dist_env()
-    if rank != 0:
-        return 0
     torch.cuda.set_device(local)
-    fastpli_gb300.native_library()
-    pool = [synth.tile(i) for i in range(args.pool)]
+    pool = [synth.tile(i) for i in range(pool_n)] if pool is None else list(pool)
+    pool_n = len(pool)
     kw = pool[0].setup_kwargs()
     rng = np.random.default_rng(5)
 
@@ -600,70 +725,102 @@ def run_serve(args):
         st = serving.latency_stats(reqs)
         st["throughput_rps"] = len(reqs) / wall
         st["batches"] = server.batches
+        st["mean_batch"] = float(np.mean([r.batch_size for r in reqs]))
         return st
 
+    results = []
     with _w.catch_warnings():
         _w.simplefilter("ignore")
-        # warm both paths (module load, autotune cache)
         warm_a, warm_s = stream_of(1000.0, 8)
-        serve(serving.ForwardServer(kw, hbm_budget=150e9, max_tiles=32, n_slots=2), warm_a, warm_s)
+        serve(serving.ForwardServer(kw, hbm_budget=150e9), warm_a, warm_s)
         serve(serving.ForwardServer(kw, hbm_budget=150e9, max_tiles=1, n_slots=1,
                                     runner=serving.PlainRunner(kw)), warm_a, warm_s)
-        results = []
-        with ClockSampler(local) as clocks:
-            for lam in args.rates:
-                n = int(min(args.max_requests, max(40, lam * args.seconds)))
-                arrivals, specs = stream_of(lam, n)
-                batched = serve(serving.ForwardServer(kw, hbm_budget=150e9, max_tiles=32,
-                                                      n_slots=2), arrivals, specs)
-                plain = serve(serving.ForwardServer(kw, hbm_budget=150e9, max_tiles=1, n_slots=1,
-                                                    runner=serving.PlainRunner(kw)),
-                              arrivals, specs)
-                results.append({"rate_rps": lam, "requests": n, "batched": batched,
-                                "plain": plain})
-    best = max(r["batched"]["throughput_rps"] for r in results)
+        for lam in rates:
+            n = int(min(max_requests, max(min_requests, lam * seconds)))
+            arrivals, specs = stream_of(lam, n)
+            batched = serve(serving.ForwardServer(kw, hbm_budget=150e9), arrivals, specs)
+            plain = serve(serving.ForwardServer(kw, hbm_budget=150e9, max_tiles=1, n_slots=1,
+                                                runner=serving.PlainRunner(kw)),
+                          arrivals, specs)
+            results.append({"rate_rps": lam, "requests": n, "batched": batched,
+                            "plain": plain})
+    return {"workload": f"Poisson arrivals, requests drawn from the first {pool_n} tiles of the "
+                        "uneven-tile mixture, 1 or 5 tilts, Slerp, epa; HBM budget 150 GB",
+            "sweep": results}
+
+
+def run_serve(args):
+    """``--workload serve``: the serving sweep alone, as its own JSON line."""
+    import torch
+    import fastpli_gb300
+    ws, rank, local = _dist_env()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    fastpli_gb300.native_library()
+    with ClockSampler(local) as clocks:
+        res = serve_sweep(args.rates, args.seconds, args.max_requests, args.min_requests,
+                          local, pool_n=args.pool)
+    best = max(r["batched"]["throughput_rps"] for r in res["sweep"])
     line = {"metric": "serving: requests/s and p50/p99 latency under Poisson load "
                       "(uneven tiles, 1 or 5 tilts, Slerp, epa)",
-            "value": best, "unit": "requests/s", "n_gpus": 1, "steps": len(results),
+            "value": best, "unit": "requests/s", "n_gpus": 1, "steps": len(res["sweep"]),
             "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"tile pool of {len(pool)} (64-512 xy, 30-120 z)",
-                       "hbm_budget_gb": 150, "max_tiles_per_batch": 32, "streams": 2},
-            "sweep": results, "clocks": clocks.summary()}
+            "config": {"workload": res["workload"], "hbm_budget_gb": 150},
+            "sweep": res["sweep"], "clocks": clocks.summary()}
     print(json.dumps(line), flush=True)
     return 0
 
 
-def max_over_ranks_ms(ms, ws, local):
-    if ws <= 1:
-        return ms
+def run_crossing(args):
+    """``--workload crossing``: the 512x512x120 volume alone, as its own line."""
     import torch
-    import torch.distributed as dist
-    if not dist.is_initialized():
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    from fastpli_gb300.shard import max_over_ranks
-    return max_over_ranks(ms, dist, device=torch.device("cuda", local))
+    import fastpli_gb300
+    ws, rank, local = _dist_env()
+    torch.cuda.set_device(local)
+    fastpli_gb300.native_library()
+    import warnings as _w
+    _w.simplefilter("ignore")
+    with ClockSampler(local) as clocks:
+        res = measure_crossing(torch.device("cuda", local), steps=args.steps,
+                               warmup=args.warmup)
+    if rank == 0:
+        line = {"metric": "ray-voxel steps/s (crossing 512x512x120: voxelize + 5 tilts x 9 "
+                          "angles, Slerp)", "value": res["steps_per_s"], "unit": UNIT,
+                "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": res["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": res["workload"]}, "detail": res,
+                "clocks": clocks.summary()}
+        print(json.dumps(line), flush=True)
+    return 0
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="crossing", choices=["crossing", "tiles", "serve"])
-    ap.add_argument("--rates", type=float, nargs="+", default=[10, 50, 200, 500],
-                    help="serve: Poisson arrival rates (requests/s)")
-    ap.add_argument("--seconds", type=float, default=4.0, help="serve: seconds per rate")
-    ap.add_argument("--max-requests", type=int, default=600, help="serve: cap per rate")
-    ap.add_argument("--pool", type=int, default=48, help="serve: distinct tiles")
-    ap.add_argument("--tiles", type=int, default=256, help="tiles of the tiles workload")
+    ap.add_argument("--workload", default="tiles", choices=["tiles", "crossing", "serve"])
+    ap.add_argument("--rates", type=float, nargs="+", default=[10, 20, 50, 100, 200, 500],
+                    help="serving: Poisson arrival rates (requests/s)")
+    ap.add_argument("--serve-seconds", type=float, default=3.0,
+                    help="tiles line: seconds of arrivals per rate of the short serving sweep "
+                         "(0 = skip)")
+    ap.add_argument("--seconds", type=float, default=20.0, help="serve: seconds per rate")
+    ap.add_argument("--min-requests", type=int, default=40, help="serve: requests per rate, min")
+    ap.add_argument("--max-requests", type=int, default=2000, help="serve: requests per rate, max")
+    ap.add_argument("--pool", type=int, default=N_TILES, help="serving: distinct tiles")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--quick", action="store_true",
+                    help="tiles line only (no crossing / watson / serving keys)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
-    if args.workload == "tiles":
-        return run_tiles(args)
+    if args.workload == "crossing":
+        return run_crossing(args)
     if args.workload == "serve":
         return run_serve(args)
     return run_gpu(args)

@@ -23,7 +23,8 @@ class BatchSizes(ctypes.Structure):
     _fields_ = [("n_tiles", ctypes.c_int64), ("n_pairs", ctypes.c_int64),
                 ("n_items", ctypes.c_int64), ("n_segments", ctypes.c_int64),
                 ("total_voxels", ctypes.c_int64), ("steps", ctypes.c_int64),
-                ("arena_bytes", ctypes.c_size_t), ("workspace_bytes", ctypes.c_size_t)]
+                ("arena_bytes", ctypes.c_size_t), ("workspace_bytes", ctypes.c_size_t),
+                ("upload_bytes", ctypes.c_size_t)]
 
 
 _P = ctypes.c_void_p
@@ -35,6 +36,8 @@ _SIGS = {
     "fpgb_batch_props": ([_P, ctypes.c_int64, _P, ctypes.c_int64], ctypes.c_int),
     "fpgb_batch_upload": ([_P, _P, _P, _P], ctypes.c_int),
     "fpgb_batch_run": ([_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P], ctypes.c_int),
+    "fpgb_batch_run_stages": ([_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P],
+                              ctypes.c_int),
     "fpgb_batch_warnings": ([_P, _P, _P, _P], ctypes.c_int),
     "fpgb_batch_destroy": ([_P], ctypes.c_int),
 }
@@ -61,13 +64,16 @@ class TileBatch:
     (e.g. ``fastpli_gb300.synth.Workload``); ``setup`` holds the keyword
     arguments of ``_Simulator.set_pli_setup``."""
 
-    def __init__(self, tiles, setup, background_mu=None, epa=False):
+    def __init__(self, tiles, setup, background_mu=None, epa=False, flat_fibers=None):
         L = lib()
         self.tiles = list(tiles)
         n = len(self.tiles)
         if n == 0:
             raise ValueError("empty batch")
-        self._flats = [N.FlatFibers(t.bundles, t.layers) for t in self.tiles]
+        # flat_fibers: the tiles' fibers already in the C ABI's flat host
+        # layout (``flatten(tiles)``), e.g. kept between batches of the same tiles
+        self._flats = (list(flat_fibers) if flat_fibers is not None
+                       else [N.FlatFibers(t.bundles, t.layers) for t in self.tiles])
         self._vols = (N.Volume * n)(*[N.make_volume(t.dim, t.origin, t.voxel_size)
                                       for t in self.tiles])
         self._fibers = (N.Fibers * n)(*[f.struct for f in self._flats])
@@ -134,12 +140,18 @@ class TileBatch:
                                         self.workspace.data_ptr(), _stream(stream)))
         return self
 
-    def run(self, ctas_per_sm=None, items_per_grab=None, coop=None, stream=None):
+    def run(self, ctas_per_sm=None, items_per_grab=None, coop=None, stream=None, stages=3):
+        """Voxelize every tile and march every pair (stages=3), or only the
+        voxelizer (1) or only the march (2)."""
         c, g, k = (tuple(self.config) + (1,))[:3]
         c = c if ctas_per_sm is None else ctas_per_sm
         g = g if items_per_grab is None else items_per_grab
         k = k if coop is None else coop
-        N.check(lib().fpgb_batch_run(self._h, int(c), int(g), int(k), _stream(stream)))
+        if stages == 3:
+            N.check(lib().fpgb_batch_run(self._h, int(c), int(g), int(k), _stream(stream)))
+        else:
+            N.check(lib().fpgb_batch_run_stages(self._h, int(stages), int(c), int(g), int(k),
+                                                _stream(stream)))
 
     def capture(self):
         """Capture the batch's launch sequence into a CUDA graph."""
@@ -204,6 +216,41 @@ class TileBatch:
         e = self.epa_block(p)
         return e[0], e[1], e[2]
 
+    def outputs_host(self, out=None, stream=None):
+        """Copies every pair's image (and epa maps) to the host in ONE
+        device-to-host copy of the arena's output region (the pairs' buffers
+        follow the tiles' volumes in the arena) into ``out`` (a page-locked
+        uint8 torch tensor of at least ``output_bytes`` bytes, allocated when
+        None), and returns (out, per-pair numpy image views)."""
+        import torch
+        lo = int(self.image_off[0])
+        nbytes = int(self.info.arena_bytes) - lo
+        if out is None:
+            out = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+        st = torch.cuda.current_stream() if stream is None else stream
+        with torch.cuda.stream(st):
+            out[:nbytes].copy_(self.arena[lo: lo + nbytes], non_blocking=True)
+        st.synchronize()
+        base = out.numpy()
+        views = []
+        for p in range(int(self.info.n_pairs)):
+            X, Y = (int(v) for v in self.tiles[self.pair_tile[p]].dim[:2])
+            o = int(self.image_off[p]) - lo
+            views.append(base[o: o + 8 * X * Y * self.n_rho].view(np.float64)
+                         .reshape(X, Y, self.n_rho))
+        return out, views
+
+    @property
+    def output_bytes(self):
+        """Bytes of the arena's image (+ epa) region that ``outputs_host`` copies."""
+        return int(self.info.arena_bytes) - int(self.image_off[0])
+
+    @property
+    def upload_bytes(self):
+        """Host-to-device bytes of ``allocate`` (segment, layer, tile and
+        march tables)."""
+        return int(self.info.upload_bytes)
+
     def pairs_of(self, t):
         return list(range(int(self.tilt_off[t]), int(self.tilt_off[t + 1])))
 
@@ -218,6 +265,11 @@ class TileBatch:
             self.close()
         except Exception:
             pass
+
+
+def flatten(tiles):
+    """The tiles' fibers in the C ABI's flat host layout (for ``flat_fibers``)."""
+    return [N.FlatFibers(t.bundles, t.layers) for t in tiles]
 
 
 def _stream(stream):

@@ -43,7 +43,7 @@ PER_FILE = {"capi.cu": ["-Xcompiler", "-fopenmp"],
             "voxel_bricks.cu": ["-fmad=false"],
             "optic.cu": ["-fmad=false"],
             "raymarch.cu": ["-fmad=false"],
-            "batch.cu": ["-fmad=false"]}
+            "batch.cu": ["-fmad=false", "-Xcompiler", "-fopenmp"]}
 
 
 def _nvcc():

@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <cstring>
 #include <memory>
+#include <string>
 #include <vector>
 
 #include "ff.cuh"
@@ -47,8 +48,9 @@ struct fpgb_batch_impl {
    std::vector<double> rotations;
    std::vector<TissuePlan> tiles;
    std::vector<TileDev> tile_dev;
-   std::vector<SegDev> segs;
-   std::vector<int32_t> seg_tile;
+   std::vector<size_t> seg_base; // first segment of each tile, n_tiles + 1 entries
+   int64_t n_segs = 0;
+   RawArray<int32_t> seg_tile;
    std::vector<LayerDev> layers;
    std::vector<MarchPlan> pairs;
    std::vector<int32_t> pair_tile;
@@ -214,10 +216,25 @@ int plan_batch(int64_t n_tiles, const fpgb_volume *vols, const fpgb_fibers *fibe
    (void)rays_per_item; // items are one CTA wide; fpgb_batch_run groups them
    B->rays_per_item = kBatchThreads;
    B->tiles.resize(n_tiles);
+   // tiles are planned in parallel (each plan runs serially inside: nested
+   // OpenMP regions get one thread); the first error in tile order wins
+   std::vector<int> rc(n_tiles, FPGB_OK);
+   std::vector<std::string> err(n_tiles);
+#pragma omp parallel for schedule(dynamic, 1)
+   for (int64_t t = 0; t < n_tiles; t++) {
+      rc[t] = plan_tissue(&vols[t], &fibers[t], &B->tiles[t]);
+      if (rc[t] != FPGB_OK)
+         err[t] = fpgb_last_error();
+   }
+   for (int64_t t = 0; t < n_tiles; t++)
+      if (rc[t] != FPGB_OK) {
+         set_error("%s", err[t].c_str());
+         return rc[t];
+      }
    int64_t vox = 0;
+   std::vector<size_t> seg_base(n_tiles + 1, 0);
    for (int64_t t = 0; t < n_tiles; t++) {
       TissuePlan &P = B->tiles[t];
-      FPGB_TRY(plan_tissue(&vols[t], &fibers[t], &P));
       if (P.X * P.Y * P.Z >= (int64_t(1) << 32)) {
          set_error("batch: tile %lld has 2^32 voxels or more", (long long)t);
          return FPGB_EINVAL;
@@ -238,10 +255,7 @@ int plan_batch(int64_t n_tiles, const fpgb_volume *vols, const fpgb_fibers *fibe
       T.max_layer = P.max_layer;
       T.layer_base = (int32_t)B->layers.size();
       B->tile_dev.push_back(T);
-      for (size_t s = 0; s < P.segs.size(); s++) {
-         B->segs.push_back(P.segs[s]);
-         B->seg_tile.push_back((int32_t)t);
-      }
+      seg_base[t + 1] = seg_base[t] + P.segs.size();
       for (int64_t b = 0; b < P.n_bundles; b++)
          B->layers.push_back(P.layers[b]);
       if (P.n_bundles == 0)
@@ -249,10 +263,20 @@ int plan_batch(int64_t n_tiles, const fpgb_volume *vols, const fpgb_fibers *fibe
       B->any_multi_bundle |= P.n_bundles > 1;
       vox += T.n_vox;
    }
-   if (B->segs.size() > 0xFFFFFFF0ull) {
+   if (seg_base[n_tiles] > 0xFFFFFFF0ull) {
       set_error("batch: too many segments");
       return FPGB_EINVAL;
    }
+   // the tiles keep their own segment tables; the upload places them one
+   // after the other (segment s of the batch belongs to the tile whose range
+   // [seg_base[t], seg_base[t+1]) holds it)
+   B->seg_base = seg_base;
+   B->n_segs = (int64_t)seg_base[n_tiles];
+   B->seg_tile.reset(seg_base[n_tiles]);
+#pragma omp parallel for schedule(dynamic, 1)
+   for (int64_t t = 0; t < n_tiles; t++)
+      std::fill(B->seg_tile.data() + seg_base[t], B->seg_tile.data() + seg_base[t + 1],
+                (int32_t)t);
    B->total_vox = vox;
 
    // (tile, tilt) pairs and their march plans
@@ -275,28 +299,54 @@ int plan_batch(int64_t n_tiles, const fpgb_volume *vols, const fpgb_fibers *fibe
       }
    }
 
-   // work items, most expensive first (rays x steps per ray)
-   for (size_t p = 0; p < B->pairs.size(); p++) {
-      const MarchParams &M = B->pairs[p].prm;
-      const int64_t rays = M.X * M.Y;
-      for (int64_t r0 = 0; r0 < rays; r0 += B->rays_per_item) {
-         BatchItem it{};
-         it.pair = (int32_t)p;
-         it.tilted = M.tilted;
-         it.ray_begin = r0;
-         it.ray_count = (int32_t)std::min<int64_t>(B->rays_per_item, rays - r0);
-         B->items.push_back(it);
+   // work items, most expensive first (rays x steps per ray) in two queues
+   // (untilted, then tilted: separate kernels), so that the dynamic queue
+   // balances well.  A pair's full 128-ray items all cost 128 n_z: the pairs
+   // are ordered by n_z and their full items emitted in that order, and the
+   // pairs' last, partial items are merged in by cost (no sort over the
+   // ~10^6 items of a large batch).
+   {
+      const int64_t R = B->rays_per_item;
+      std::vector<int32_t> order(B->pairs.size());
+      for (size_t p = 0; p < order.size(); p++)
+         order[p] = (int32_t)p;
+      auto tilted = [&](int32_t p) { return B->pairs[p].prm.tilted; };
+      auto nz = [&](int32_t p) { return (int64_t)B->pairs[p].prm.n_z; };
+      std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
+         if (tilted(a) != tilted(b))
+            return tilted(a) < tilted(b);
+         return nz(a) > nz(b);
+      });
+      struct Keyed {
+         int64_t cost;
+         BatchItem it;
+      };
+      std::vector<Keyed> full[2], part[2];
+      for (int32_t p : order) {
+         const MarchParams &M = B->pairs[p].prm;
+         const int64_t rays = M.X * M.Y;
+         const int tl = M.tilted ? 1 : 0;
+         for (int64_t r0 = 0; r0 < rays; r0 += R) {
+            BatchItem it{};
+            it.pair = p;
+            it.tilted = M.tilted;
+            it.ray_begin = r0;
+            it.ray_count = (int32_t)std::min<int64_t>(R, rays - r0);
+            (it.ray_count == R ? full : part)[tl].push_back({it.ray_count * nz(p), it});
+         }
+      }
+      auto by_cost = [](const Keyed &a, const Keyed &b) { return a.cost > b.cost; };
+      B->items.clear();
+      B->items.reserve(full[0].size() + full[1].size() + part[0].size() + part[1].size());
+      for (int tl = 0; tl < 2; tl++) {
+         std::stable_sort(part[tl].begin(), part[tl].end(), by_cost);
+         std::vector<Keyed> merged(full[tl].size() + part[tl].size());
+         std::merge(full[tl].begin(), full[tl].end(), part[tl].begin(), part[tl].end(),
+                    merged.begin(), by_cost);
+         for (const Keyed &k : merged)
+            B->items.push_back(k.it);
       }
    }
-   // two queues (untilted items, then tilted items: separate kernels), each
-   // ordered by decreasing cost so that the dynamic queue balances well
-   std::stable_sort(B->items.begin(), B->items.end(), [&](const BatchItem &a, const BatchItem &b) {
-      if (a.tilted != b.tilted)
-         return a.tilted < b.tilted;
-      const int64_t ca = (int64_t)a.ray_count * B->pairs[a.pair].prm.n_z;
-      const int64_t cb = (int64_t)b.ray_count * B->pairs[b.pair].prm.n_z;
-      return ca > cb;
-   });
    B->n_untilted = 0;
    while (B->n_untilted < (int64_t)B->items.size() && !B->items[B->n_untilted].tilted)
       B->n_untilted++;
@@ -318,7 +368,7 @@ int plan_batch(int64_t n_tiles, const fpgb_volume *vols, const fpgb_fibers *fibe
    // workspace
    size_t w = 0;
    B->ws_bricks = take(w, brick_workspace_bytes(B->n_bricks, B->brick_pairs));
-   B->ws_segs = take(w, sizeof(SegDev) * B->segs.size());
+   B->ws_segs = take(w, sizeof(SegDev) * B->n_segs);
    B->ws_segtile = take(w, sizeof(int32_t) * B->seg_tile.size());
    B->ws_layers = take(w, sizeof(LayerDev) * B->layers.size());
    B->ws_tiles = take(w, sizeof(TileDev) * B->tile_dev.size() + 2 * sizeof(void *) * n_tiles);
@@ -344,8 +394,12 @@ int upload_batch(fpgb_batch_impl *B, void *arena, void *ws, cudaStream_t st) {
    B->arena = static_cast<char *>(arena);
    B->ws = static_cast<char *>(ws);
    char *W = B->ws;
-   FPGB_CUDA_TRY(cudaMemcpyAsync(W + B->ws_segs, B->segs.data(), sizeof(SegDev) * B->segs.size(),
-                                 cudaMemcpyHostToDevice, st));
+   for (size_t t = 0; t < B->tiles.size(); t++)
+      if (!B->tiles[t].segs.empty())
+         FPGB_CUDA_TRY(cudaMemcpyAsync(W + B->ws_segs + sizeof(SegDev) * B->seg_base[t],
+                                       B->tiles[t].segs.data(),
+                                       sizeof(SegDev) * B->tiles[t].segs.size(),
+                                       cudaMemcpyHostToDevice, st));
    FPGB_CUDA_TRY(cudaMemcpyAsync(W + B->ws_segtile, B->seg_tile.data(),
                                  sizeof(int32_t) * B->seg_tile.size(), cudaMemcpyHostToDevice, st));
    FPGB_CUDA_TRY(cudaMemcpyAsync(W + B->ws_layers, B->layers.data(),
@@ -361,17 +415,22 @@ int upload_batch(fpgb_batch_impl *B, void *arena, void *ws, cudaStream_t st) {
    }
    FPGB_CUDA_TRY(cudaMemcpyAsync(W + B->ws_tiles, tiles.data(), tiles.size(),
                                  cudaMemcpyHostToDevice, st));
-   // per-pair parameter blocks with their tables and buffers bound
+   // per-pair parameter blocks with their tables and buffers bound; the
+   // pairs' tables are staged on the host and go up in one copy
    std::vector<MarchParams> prm(B->pairs.size());
+   size_t tab_bytes = 0;
+   for (size_t p = 0; p < B->pairs.size(); p++)
+      tab_bytes = std::max(tab_bytes, B->table_off[p] + march_table_bytes(B->pairs[p]));
+   std::vector<char> tab(tab_bytes);
    for (size_t p = 0; p < B->pairs.size(); p++) {
       const MarchPlan &mp = B->pairs[p];
       MarchParams M = mp.prm;
       char *tb = W + B->ws_tables + B->table_off[p];
-      FPGB_CUDA_TRY(cudaMemcpyAsync(tb, mp.lut.data(), sizeof(LabelOptics) * mp.lut.size(),
-                                    cudaMemcpyHostToDevice, st));
       char *zt = tb + align_up(sizeof(LabelOptics) * mp.lut.size(), 256);
-      FPGB_CUDA_TRY(cudaMemcpyAsync(zt, mp.ztab.data(), sizeof(ZStep) * mp.ztab.size(),
-                                    cudaMemcpyHostToDevice, st));
+      std::memcpy(tab.data() + B->table_off[p], mp.lut.data(),
+                  sizeof(LabelOptics) * mp.lut.size());
+      std::memcpy(tab.data() + (zt - (W + B->ws_tables)), mp.ztab.data(),
+                  sizeof(ZStep) * mp.ztab.size());
       M.lut = reinterpret_cast<const LabelOptics *>(tb);
       M.ztab = reinterpret_cast<const ZStep *>(zt);
       const int t = B->pair_tile[p];
@@ -389,6 +448,9 @@ int upload_batch(fpgb_batch_impl *B, void *arena, void *ws, cudaStream_t st) {
       }
       prm[p] = M;
    }
+   if (tab_bytes)
+      FPGB_CUDA_TRY(cudaMemcpyAsync(W + B->ws_tables, tab.data(), tab_bytes,
+                                    cudaMemcpyHostToDevice, st));
    FPGB_CUDA_TRY(cudaMemcpyAsync(W + B->ws_prm, prm.data(), sizeof(MarchParams) * prm.size(),
                                  cudaMemcpyHostToDevice, st));
    FPGB_CUDA_TRY(cudaMemcpyAsync(W + B->ws_items, B->items.data(),
@@ -416,8 +478,10 @@ int upload_batch(fpgb_batch_impl *B, void *arena, void *ws, cudaStream_t st) {
 
 
 // All device work of one batch: no allocation, no host synchronisation, so
-// a stream capture of this call is a complete graph of the batch.
-int run_batch(fpgb_batch_impl *B, int march_ctas_per_sm, int chunk, int coop, cudaStream_t st) {
+// a stream capture of this call is a complete graph of the batch.  stages:
+// bit 0 the voxelizer, bit 1 the march (which reads the voxelizer's output).
+int run_batch(fpgb_batch_impl *B, int march_ctas_per_sm, int chunk, int coop, cudaStream_t st,
+              int stages = 3) {
    if (!B->arena || !B->ws) {
       set_error("batch: buffers not bound (call fpgb_batch_upload first)");
       return FPGB_EINVAL;
@@ -436,11 +500,18 @@ int run_batch(fpgb_batch_impl *B, int march_ctas_per_sm, int chunk, int coop, cu
    auto *counters = reinterpret_cast<unsigned long long *>(W + B->ws_counters);
    unsigned long long *next = counters + kCounterWords;
 
-   FPGB_CUDA_TRY(cudaMemsetAsync(counters, 0, sizeof(unsigned long long) * (kCounterWords + 2),
-                                 st));
-   FPGB_TRY(launch_voxel_bricks(segs, seg_tile, (int64_t)B->segs.size(), tiles, (int64_t)nt,
-                                B->n_bricks, B->brick_pairs, layers, B->any_multi_bundle, lptr,
-                                vptr, W + B->ws_bricks, counters, st));
+   if (stages & 1) {
+      FPGB_CUDA_TRY(cudaMemsetAsync(counters, 0,
+                                    sizeof(unsigned long long) * (kCounterWords + 2), st));
+      FPGB_TRY(launch_voxel_bricks(segs, seg_tile, B->n_segs, tiles, (int64_t)nt,
+                                   B->n_bricks, B->brick_pairs, layers, B->any_multi_bundle,
+                                   lptr, vptr, W + B->ws_bricks, counters, st));
+   } else {
+      // the march's queue counters only: the voxelizer's warnings stay
+      FPGB_CUDA_TRY(cudaMemsetAsync(next, 0, sizeof(unsigned long long) * 2, st));
+   }
+   if (!(stages & 2))
+      return FPGB_OK;
    const int64_t n0 = B->n_untilted, n1 = (int64_t)B->items.size() - B->n_untilted;
    const int ch = chunk > 0 ? chunk : 4;
 #define FPGB_BATCH_MARCH(M)                                                                    \
@@ -490,11 +561,18 @@ int fpgb_batch_info(const fpgb_batch *b, fpgb_batch_sizes *info) {
    info->n_tiles = (int64_t)b->tiles.size();
    info->n_pairs = (int64_t)b->pairs.size();
    info->n_items = (int64_t)b->items.size();
-   info->n_segments = (int64_t)b->segs.size();
+   info->n_segments = b->n_segs;
    info->total_voxels = b->total_vox;
    info->steps = b->steps;
    info->arena_bytes = b->arena_bytes;
    info->workspace_bytes = b->ws_bytes;
+   size_t up = sizeof(SegDev) * b->n_segs + sizeof(int32_t) * b->seg_tile.size() +
+               sizeof(LayerDev) * b->layers.size() +
+               (sizeof(TileDev) + 2 * sizeof(void *)) * b->tile_dev.size() +
+               sizeof(MarchParams) * b->pairs.size() + sizeof(BatchItem) * b->items.size();
+   for (const MarchPlan &mp : b->pairs)
+      up += sizeof(LabelOptics) * mp.lut.size() + sizeof(ZStep) * mp.ztab.size();
+   info->upload_bytes = up;
    return FPGB_OK;
 }
 
@@ -550,6 +628,15 @@ int fpgb_batch_run(fpgb_batch *b, int march_ctas_per_sm, int items_per_grab, int
       return FPGB_EINVAL;
    }
    return run_batch(b, march_ctas_per_sm, items_per_grab, march_coop, as_stream(stream));
+}
+
+int fpgb_batch_run_stages(fpgb_batch *b, int stages, int march_ctas_per_sm, int items_per_grab,
+                          int march_coop, void *stream) {
+   if (!b || stages < 1 || stages > 3) {
+      set_error("batch: null handle or stages not in 1..3");
+      return FPGB_EINVAL;
+   }
+   return run_batch(b, march_ctas_per_sm, items_per_grab, march_coop, as_stream(stream), stages);
 }
 
 int fpgb_batch_warnings(const fpgb_batch *b, fpgb_warnings *w, int64_t *fp64_replays,

@@ -196,16 +196,28 @@ def wide_strip(seed=41):
                     tilts=np.deg2rad([(0, 0), (10, 90)]))
 
 
+def _tile_draws(rng):
+    X, Y = (int(v) for v in rng.integers(64, 513, 2))
+    Z = int(rng.integers(30, 121))
+    nf = int(rng.integers(50, 2001))
+    dn = float(rng.uniform(-0.004, 0.004))
+    mu = float(rng.uniform(0.0, 20.0))
+    return (X, Y, Z), nf, dn, mu
+
+
+def tile_params(i, seed_base=1000):
+    """(dim, fibers, dn, mu) of tile ``i`` of the uneven-tile mixture without
+    generating its fibers."""
+    return _tile_draws(np.random.default_rng(seed_base + i))
+
+
 def tile(i, seed_base=1000, n_fibers=None, segment_um=2.0):
     """Tile ``i`` of the uneven-tile mixture."""
     rng = np.random.default_rng(seed_base + i)
-    X, Y = (int(v) for v in rng.integers(64, 513, 2))
-    Z = int(rng.integers(30, 121))
+    (X, Y, Z), nf, dn, mu = _tile_draws(rng)
     vs = 0.2
     size = np.array([X, Y, Z]) * vs
-    nf = int(rng.integers(50, 2001)) if n_fibers is None else int(n_fibers)
-    dn = float(rng.uniform(-0.004, 0.004))
-    mu = float(rng.uniform(0.0, 20.0))
+    nf = nf if n_fibers is None else int(n_fibers)
     v = rng.normal(size=(nf, 3))
     v /= np.linalg.norm(v, axis=1, keepdims=True)
     fibers = []

@@ -38,6 +38,7 @@ typedef struct fpgb_batch_sizes {
    int64_t steps;    /* ray-voxel steps of all pairs */
    size_t arena_bytes;     /* outputs: labels, vectors, images (+ epa) */
    size_t workspace_bytes; /* keys, tables, queue */
+   size_t upload_bytes;    /* host-to-device bytes of fpgb_batch_upload */
 } fpgb_batch_sizes;
 
 /* Tile t: vols[t], fibers[t], background absorption background_mu[t] (props
@@ -69,6 +70,12 @@ int fpgb_batch_upload(fpgb_batch *b, void *d_arena, void *d_workspace,
  * fastpli_gb300.autotune picks them. */
 int fpgb_batch_run(fpgb_batch *b, int march_ctas_per_sm, int items_per_grab,
                    int march_coop, void *stream);
+/* One stage of fpgb_batch_run: stages = 1 the voxelizer only, 2 the march
+ * only (of the volumes the last voxelizer run left in the arena), 3 both
+ * (= fpgb_batch_run).  Lets a caller time or overlap the two stages
+ * separately; the results are those of fpgb_batch_run. */
+int fpgb_batch_run_stages(fpgb_batch *b, int stages, int march_ctas_per_sm,
+                          int items_per_grab, int march_coop, void *stream);
 /* Synchronises; fails with FPGB_EINVAL when a label was out of range.
  * fp64_replays (may be NULL) counts voxelizer candidates decided in FP64. */
 int fpgb_batch_warnings(const fpgb_batch *b, fpgb_warnings *w,

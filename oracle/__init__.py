@@ -157,6 +157,37 @@ def generate(dim, origin, voxel_size, fiber_bundles, layers, only_label=False,
 _INTERP = {"NN": 0, "Lerp": 1, "Slerp": 2}
 
 
+def _pi_case_cos(v):
+    """vm::rot_pi_cases::cos (src/include/vemath.hpp:510-520)."""
+    import math
+    v = math.fmod(v, 2 * math.pi)
+    if v == 0:
+        return 1.0
+    if v in (math.pi / 2, math.pi + math.pi / 2, -math.pi / 2, -(math.pi + math.pi / 2)):
+        return 0.0
+    if v in (math.pi, -math.pi):
+        return -1.0
+    return math.cos(v)
+
+
+def count_steps(dim, theta, step_size=1.0):
+    """Ray-voxel steps of one run_simulation call, on the host: X * Y rays,
+    each stepping from z = step_z / 2 in steps of step_z = cos(theta) *
+    step_size while floor(z) lies in [0, Z) (src/simulation/simulator.cpp:
+    216-231 with LightDirectionUnitVector :585-590, and the loop :259-261)."""
+    import math
+    X, Y, Z = (int(v) for v in np.asarray(dim).reshape(3))
+    dz = _pi_case_cos(float(theta)) * float(step_size)
+    if not dz > 0:
+        raise ValueError("light direction has no positive z component")
+    n = 0
+    z = 0.0 + dz * 0.5
+    while math.floor(z) >= 0 and math.floor(z) < Z:
+        n += 1
+        z = z + dz
+    return X * Y * n
+
+
 def simulate(label, vector, props, theta=0.0, phi=0.0, *, step_size=1.0,
              light_intensity=26000.0, voxel_size=1.0, wavelength=525.0,
              tissue_refrection=1.0, interpolate="Slerp",

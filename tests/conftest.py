@@ -14,6 +14,19 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
 
 
+def pytest_terminal_summary(terminalreporter):
+    """The max errors every parity test measured, printed at the end of the
+    run (also in -q mode), and written as JSON to $FPGB_PARITY_REPORT."""
+    import json
+    import parity
+    for line in parity.summary_lines():
+        terminalreporter.write_line(line)
+    path = os.environ.get("FPGB_PARITY_REPORT")
+    if path and parity.REPORT:
+        with open(path, "w") as f:
+            json.dump(parity.REPORT, f, indent=1, sort_keys=True)
+
+
 @pytest.fixture(scope="session")
 def oracle_port():
     """The C restatement of the reference (test infrastructure only)."""

@@ -76,3 +76,40 @@ def test_full_size_matches_reference(cuda, name):
         rel = np.abs(sub - ref) / np.abs(ref)
         assert rel.max() < 1e-4, (name, k, rel.max())
         assert abs(float(img.mean()) / e["image_mean"][k] - 1) < 1e-5
+
+
+@pytest.mark.gpu
+def test_crossing_every_pixel_of_every_bench_tilt_vs_oracle(cuda, oracle_port):
+    """The bench volume (512 x 512 x 120, 2 x 1000 fibers) at all 5 bench
+    tilts, every pixel and polarizer angle, against the FP64 oracle run in
+    the test (the oracle is pinned bit for bit to the reference's build)."""
+    import parity
+    torch = cuda
+    from fastpli_gb300.simulation import _Generator, _Simulator
+    threads = os.cpu_count() or 1
+    w = synth.crossing()
+    olab, ovec, oprops, _ = oracle_port.generate(w.dim, w.origin, w.voxel_size, w.bundles,
+                                                 w.layers, n_threads=threads)
+    g = _Generator()
+    g.set_volume(w.dim, w.origin, w.voxel_size)
+    g.set_fiber_bundles(w.bundles, w.layers)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        lab, vec, props, _ = g.run_generation_device()
+    torch.cuda.synchronize()
+    n_lab = int((lab.cpu().numpy() != olab).sum())
+    n_vec = int((vec.cpu().numpy().view(np.uint32) != ovec.view(np.uint32)).sum())
+    assert n_lab == 0 and n_vec == 0
+    kw = w.setup_kwargs()
+    sim = _Simulator()
+    sim.set_pli_setup(kw["step_size"], kw["light_intensity"], kw["voxel_size"], kw["wavelength"],
+                      kw["tissue_refrection"], kw["interpolate"], kw["untilt_sensor_view"],
+                      kw["flip_z"], kw["filter_rotations"])
+    for k, (t, p) in enumerate(w.tilts):
+        img = sim.run_simulation_device(w.dim, lab, vec, props, float(t), float(p))
+        ref, _ = oracle_port.simulate(olab, ovec, oprops, float(t), float(p), n_threads=threads,
+                                      **kw)
+        e = parity.image_errors(img.cpu().numpy(), ref)
+        parity.record(f"crossing512/tilt{k}", label_mismatch=n_lab, vector_mismatch=n_vec,
+                      pixels=int(ref.size), **e)
+        assert e["max_rel"] <= parity.IMG_RTOL, (k, e)

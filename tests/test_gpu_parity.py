@@ -1,12 +1,12 @@
 """GPU parity: the CUDA voxelizer and ray march, called through the C ABI,
 against the reference's golden fixtures and the oracle.
 
-Bars (stated per result, max error reported):
+Bars (tests/parity.py; the max error of every result is recorded and printed
+at the end of the run):
   * labels: bit-exact; vectors: bit-exact (float32 bits);
   * images: relative error <= 1e-4 per pixel (FP32 march vs FP64 reference);
   * epa transmittance/retardation <= 1e-3 relative, direction <= 1e-3 rad
     (mod pi).
-Set FPGB_PARITY_REPORT=<path> to write the max errors as JSON.
 """
 
 import hashlib
@@ -22,18 +22,7 @@ from fastpli_gb300.simulation import _Generator, _Simulator
 
 pytestmark = pytest.mark.gpu
 
-IMG_RTOL = 1e-4
-EPA_TOL = 1e-3
-REPORT = {}
-
-
-@pytest.fixture(scope="module", autouse=True)
-def _report():
-    yield
-    path = os.environ.get("FPGB_PARITY_REPORT")
-    if path:
-        with open(path, "w") as f:
-            json.dump(REPORT, f, indent=1, sort_keys=True)
+from parity import EPA_TOL, IMG_RTOL, REPORT  # noqa: E402
 
 
 def _gold(name):
@@ -59,11 +48,7 @@ def _simulator(kw):
     return s
 
 
-def _rel(a, b):
-    a = np.asarray(a, np.float64)
-    b = np.asarray(b, np.float64)
-    den = np.maximum(np.abs(b), 1e-300)
-    return float(np.max(np.abs(a - b) / den)) if a.size else 0.0
+from parity import rel as _rel  # noqa: E402
 
 
 def _check_images(key, got, ref):

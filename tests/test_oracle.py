@@ -155,3 +155,20 @@ def test_port_rejects_invalid_input(oracle_port):
         oracle_port.simulate(g["label"], g["vector"], g["props"][:2], 0, 0)
     with pytest.raises(ValueError, match="step_size"):
         oracle_port.simulate(g["label"], g["vector"], g["props"], 0, 0, step_size=0)
+
+
+def test_step_count_on_the_host_matches_the_library():
+    """oracle.count_steps (the reference's z loop replayed in Python, used by
+    the CPU arm of bench.py, which loads nothing of the product) agrees with
+    the library's planner."""
+    import oracle
+    from fastpli_gb300 import _native as N
+    lib = N.load()
+    for dim in ((512, 512, 120), (64, 80, 30), (3, 5, 7), (100, 7, 119)):
+        for step in (1.0, 0.7, 1.0 / np.cos(np.deg2rad(5.5))):
+            for th, ph in np.deg2rad([(0, 0), (5.5, 0), (5.5, 270), (30, 45), (60, 200)]):
+                s = N.SetupBlock(step, 26000.0, 0.2, 525.0, 1.0, "Slerp", True, False,
+                                 np.deg2rad([0, 90]))
+                d = np.asarray(dim, np.int64)
+                want = int(lib.fpgb_count_steps(N.byref(s.struct), N.ptr(d), float(th), float(ph)))
+                assert oracle.count_steps(dim, th, step) == want, (dim, step, th)

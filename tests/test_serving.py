@@ -134,12 +134,17 @@ def test_result_same_alone_and_in_mix(cuda):
     for i, t in enumerate(tiles):
         t.dim = np.array([24 + 7 * i, 31, 11 + 3 * i])
     kw = tiles[0].setup_kwargs()
+    with serving.ForwardServer(kw, hbm_budget=8e9, max_tiles=8, n_slots=2) as srv:
+        alone = srv.submit(tiles[2], tiles[2].tilts)
+        alone_out = alone.wait(60)
+    assert alone.batch_size == 1  # the plain per-call kernels
+    # the mix is queued before the server thread starts, so it is admitted as
+    # one batch: the request compared below runs in the batched kernels
     srv = serving.ForwardServer(kw, hbm_budget=8e9, max_tiles=8, n_slots=2)
+    mix = [srv.submit(t, t.tilts[: 1 + (i % 5)]) for i, t in enumerate(tiles)]
+    mix.append(srv.submit(tiles[2], tiles[2].tilts))
     with srv:
-        alone = srv.submit(tiles[2], tiles[2].tilts).wait(60)
-        mix = [srv.submit(t, t.tilts[: 1 + (i % 5)]) for i, t in enumerate(tiles)]
-        mix.append(srv.submit(tiles[2], tiles[2].tilts))
         out = [r.wait(60) for r in mix]
-    assert max(r.batch_size for r in mix) > 1
-    for (ta, da, ra), (tb, db, rb) in zip(alone["epa"], out[-1]["epa"]):
+    assert mix[-1].batch_size == len(mix)
+    for (ta, da, ra), (tb, db, rb) in zip(alone_out["epa"], out[-1]["epa"]):
         assert np.array_equal(ta, tb) and np.array_equal(da, db) and np.array_equal(ra, rb)
