@@ -348,13 +348,16 @@ def run_gpu(args):
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream()
 
-    all_params = [synth.tile_params(i) for i in range(N_TILES)]
+    all_params = [synth.tile_params(i) for i in range(args.tiles)]
     mine = rank_units([int(np.prod(p[0])) for p in all_params], ws, rank)
     tiles = [synth.tile(i) for i in mine]
     kw = tiles[0].setup_kwargs()
     flats = B.flatten(tiles)
     b = B.TileBatch(tiles, kw, flat_fibers=flats).allocate()
-    cfg, _, _ = autotune.tune(b, reps=1)
+    if args.no_tune:
+        cfg = b.config = (0, 2, 1, 0)
+    else:
+        cfg, _, _ = autotune.tune(b, reps=1)
     b.capture()
     steps = b.steps
     n_pairs = int(b.info.n_pairs)
@@ -524,12 +527,12 @@ def run_gpu(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"uneven tile batch, {N_TILES} tiles (xy 64-512, z 30-120 "
+            "config": {"workload": f"uneven tile batch, {args.tiles} tiles (xy 64-512, z 30-120 "
                                    f"@ 0.2 um, 50-2000 fibers, 5 tilts x 9 angles, Slerp)",
                        "tiles": len(tiles), "voxels": vox, "pairs": n_pairs,
                        "ray_voxel_steps": steps, "graph": "CUDA graph replay",
                        "march_config": {"ctas_per_sm": cfg[0], "items_per_grab": cfg[1],
-                                        "coop": cfg[2]},
+                                        "coop": cfg[2], "ray_block": B.TileBatch.SHAPES[cfg[3]]},
                        "l2": f"inputs larger than L2 ({vox_bytes / 1e9:.1f} GB of fields)",
                        "parallelism": f"replicas x{ws} (tiles sharded)"},
             "tissue_voxels_per_s": vox / (vox_ms * 1e-3),
@@ -814,6 +817,10 @@ def main():
     ap.add_argument("--max-requests", type=int, default=2000, help="serve: requests per rate, max")
     ap.add_argument("--pool", type=int, default=N_TILES, help="serving: distinct tiles")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--tiles", type=int, default=N_TILES,
+                    help="tiles of the batch (the first n of the mixture; smaller for profiling)")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="skip the autotuner (fixed launch configuration; for profiling)")
     ap.add_argument("--quick", action="store_true",
                     help="tiles line only (no crossing / watson / serving keys)")
     args = ap.parse_args()

@@ -38,6 +38,7 @@ _SIGS = {
     "fpgb_batch_run": ([_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P], ctypes.c_int),
     "fpgb_batch_run_stages": ([_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P],
                               ctypes.c_int),
+    "fpgb_batch_set_shape": ([_P, ctypes.c_int, _P], ctypes.c_int),
     "fpgb_batch_warnings": ([_P, _P, _P, _P], ctypes.c_int),
     "fpgb_batch_destroy": ([_P], ctypes.c_int),
 }
@@ -111,7 +112,8 @@ class TileBatch:
         self.arena = None
         self.workspace = None
         self._graph = None
-        self.config = (0, 0, 1)
+        self.shape = 0
+        self.config = (0, 0, 1, 0)
 
     # ------------------------------------------------------------ sizes ---
     @property
@@ -140,13 +142,28 @@ class TileBatch:
                                         self.workspace.data_ptr(), _stream(stream)))
         return self
 
-    def run(self, ctas_per_sm=None, items_per_grab=None, coop=None, stream=None, stages=3):
+    SHAPES = ("128 consecutive rays", "2 x 64 rays", "4 x 32 rays", "8 x 16 rays")
+
+    def set_shape(self, shape, stream=None):
+        """Ray-block shape of the march's work items (``SHAPES``); results do
+        not depend on it.  A captured graph is dropped (capture again)."""
+        shape = int(shape)
+        if shape != self.shape:
+            N.check(lib().fpgb_batch_set_shape(self._h, shape, _stream(stream)))
+            self.shape = shape
+            self._graph = None
+
+    def run(self, ctas_per_sm=None, items_per_grab=None, coop=None, stream=None, stages=3,
+            shape=None):
         """Voxelize every tile and march every pair (stages=3), or only the
-        voxelizer (1) or only the march (2)."""
-        c, g, k = (tuple(self.config) + (1,))[:3]
+        voxelizer (1) or only the march (2).  Launch knobs default to
+        ``config`` = (ctas_per_sm, items_per_grab, coop, shape)."""
+        cfg = list(self.config) + [0, 0, 1, 0][len(self.config):]
+        c, g, k, sh = cfg[:4]
         c = c if ctas_per_sm is None else ctas_per_sm
         g = g if items_per_grab is None else items_per_grab
         k = k if coop is None else coop
+        self.set_shape(sh if shape is None else shape, stream)
         if stages == 3:
             N.check(lib().fpgb_batch_run(self._h, int(c), int(g), int(k), _stream(stream)))
         else:

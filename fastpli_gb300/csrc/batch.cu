@@ -31,15 +31,22 @@
 namespace fpgb {
 
 
-// A work item: 128 consecutive rays of one (tile, tilt) pair.  (Rays in
-// 4 x 32 tiles, as the plain kernel marches them, idle up to 31 lanes per tile
-// row on tiles whose width is not a multiple of 32: 3% slower on the 256-tile
-// mix.)
+// A work item: one block of 128 rays of one (tile, tilt) pair.  Its shape is
+// a launch parameter the autotuner picks: shape 0 is 128 consecutive rays in
+// the ray order x * Y + y (lines along y that wrap to the next x: no idle
+// lanes but on the last block of a pair); shape s = 1, 2, 3 is a rectangle
+// of 2^s x (128 >> s) rays, x by y (neighbouring rays in x share more of the
+// 8-corner neighbourhoods of a tilted march; idle lanes where the rectangle
+// overhangs the tile).  ray_begin is the first ray (shape 0) or the
+// rectangle's corner ray x0 * Y + y0.
+constexpr int kItemShapes = 4;
+
 struct BatchItem {
    int32_t pair;
    int32_t tilted;
    int64_t ray_begin;
-   int32_t ray_count;
+   int32_t ray_count; // shape 0: rays of the block
+   int32_t x0, y0;    // shape > 0: the rectangle's corner
    int32_t pad_;
 };
 
@@ -69,6 +76,8 @@ struct fpgb_batch_impl {
    // bound buffers
    char *arena = nullptr, *ws = nullptr;
    int rays_per_item = 0;
+   int shape = 0;          // ray-block shape of the items (BatchItem)
+   size_t max_items = 0;   // items of the shape with the most (sizes ws_items)
    int64_t n_untilted = 0; // items [0, n_untilted) untilted, the rest tilted
    int sms = 1;
    int fit[2][2] = {{1, 1}, {1, 1}}; // resident CTAs per SM: [untilted / tilted][per-thread / coop]
@@ -88,7 +97,7 @@ template <int MODE, bool TILT, bool COOP, bool WIDE>
 __global__ void __launch_bounds__(128)
 batch_march(const MarchParams *__restrict__ prm, const BatchItem *__restrict__ items,
             int64_t n_items, int chunk, unsigned long long *__restrict__ next,
-            unsigned long long *__restrict__ counters) {
+            unsigned long long *__restrict__ counters, int shape) {
    __shared__ unsigned long long s_item;
    // the item's parameter block, staged in shared memory (read like the
    // plain kernel reads its by-value parameters)
@@ -115,8 +124,18 @@ batch_march(const MarchParams *__restrict__ prm, const BatchItem *__restrict__ i
             cur = w.pair;
             __syncthreads();
          }
-         const int64_t ray = w.ray_begin + threadIdx.x;
-         const bool valid = (int)threadIdx.x < w.ray_count;
+         int64_t ray;
+         bool valid;
+         if (shape == 0) {
+            ray = w.ray_begin + threadIdx.x;
+            valid = (int)threadIdx.x < w.ray_count;
+         } else { // 2^shape x (128 >> shape) rectangle, y fastest
+            const int dx = (int)threadIdx.x >> (7 - shape);
+            const int dy = (int)threadIdx.x & ((kBatchThreads >> shape) - 1);
+            const int64_t x = (int64_t)w.x0 + dx, y = (int64_t)w.y0 + dy;
+            valid = x < sP.X && y < sP.Y;
+            ray = valid ? x * sP.Y + y : w.ray_begin;
+         }
          if (!TILT && sP.column) {
             if (valid)
                march_one_ray_column(sP, ray, sP.label, sP.vec, sP.image, sP.epa_t, sP.epa_d,
@@ -153,7 +172,7 @@ template <int MODE, bool TILT>
 int launch_batch_march(const MarchParams *prm, const BatchItem *items, int64_t n_items,
                        unsigned long long *next, unsigned long long *counters, int sms,
                        const int fits[2], int ctas_per_sm, int chunk, int coop, bool narrow,
-                       cudaStream_t st) {
+                       int shape, cudaStream_t st) {
    if (n_items <= 0)
       return FPGB_OK;
    const bool cp = MODE != 0 && coop != 0;
@@ -161,8 +180,8 @@ int launch_batch_march(const MarchParams *prm, const BatchItem *items, int64_t n
    const int per_sm = std::max(1, std::min(ctas_per_sm > 0 ? ctas_per_sm : fit, fit));
    const int64_t grid = std::min<int64_t>((int64_t)sms * per_sm, (n_items + chunk - 1) / chunk);
 #define FPGB_BM(C, W)                                                                         \
-   batch_march<MODE, TILT, C, W><<<(unsigned)grid, kBatchThreads, 0, st>>>(prm, items, n_items, \
-                                                                           chunk, next, counters)
+   batch_march<MODE, TILT, C, W><<<(unsigned)grid, kBatchThreads, 0, st>>>(                    \
+       prm, items, n_items, chunk, next, counters, shape)
    if (cp) {
       if (narrow)
          FPGB_BM(true, false);
@@ -195,6 +214,75 @@ size_t take(size_t &cursor, size_t bytes) {
    const size_t at = cursor;
    cursor += align_up(std::max<size_t>(bytes, 1), 256);
    return at;
+}
+
+// Work items of ray-block shape `shape` (BatchItem), most expensive first
+// (rays x steps per ray) in two queues (untilted, then tilted: separate
+// kernels), so that the dynamic queue balances well.  A pair's full blocks
+// all cost 128 n_z: the pairs are ordered by n_z and their full blocks
+// emitted in that order, and the blocks that overhang the tile are merged in
+// by cost (no sort over the ~10^6 items of a large batch).
+void make_items(fpgb_batch_impl *B, int shape) {
+   const int64_t R = B->rays_per_item;
+   const int64_t tx = int64_t(1) << shape, ty = R >> shape;
+   std::vector<int32_t> order(B->pairs.size());
+   for (size_t p = 0; p < order.size(); p++)
+      order[p] = (int32_t)p;
+   auto tilted = [&](int32_t p) { return B->pairs[p].prm.tilted; };
+   auto nz = [&](int32_t p) { return (int64_t)B->pairs[p].prm.n_z; };
+   std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
+      if (tilted(a) != tilted(b))
+         return tilted(a) < tilted(b);
+      return nz(a) > nz(b);
+   });
+   struct Keyed {
+      int64_t cost;
+      BatchItem it;
+   };
+   std::vector<Keyed> full[2], part[2];
+   for (int32_t p : order) {
+      const MarchParams &M = B->pairs[p].prm;
+      const int tl = M.tilted ? 1 : 0;
+      if (shape == 0) {
+         const int64_t rays = M.X * M.Y;
+         for (int64_t r0 = 0; r0 < rays; r0 += R) {
+            BatchItem it{};
+            it.pair = p;
+            it.tilted = M.tilted;
+            it.ray_begin = r0;
+            it.ray_count = (int32_t)std::min<int64_t>(R, rays - r0);
+            (it.ray_count == R ? full : part)[tl].push_back({it.ray_count * nz(p), it});
+         }
+      } else {
+         for (int64_t x0 = 0; x0 < M.X; x0 += tx)
+            for (int64_t y0 = 0; y0 < M.Y; y0 += ty) {
+               BatchItem it{};
+               it.pair = p;
+               it.tilted = M.tilted;
+               it.x0 = (int32_t)x0;
+               it.y0 = (int32_t)y0;
+               it.ray_begin = x0 * M.Y + y0;
+               const int64_t n = std::min(tx, M.X - x0) * std::min(ty, M.Y - y0);
+               it.ray_count = (int32_t)n;
+               (n == R ? full : part)[tl].push_back({n * nz(p), it});
+            }
+      }
+   }
+   auto by_cost = [](const Keyed &a, const Keyed &b) { return a.cost > b.cost; };
+   B->items.clear();
+   B->items.reserve(full[0].size() + full[1].size() + part[0].size() + part[1].size());
+   for (int tl = 0; tl < 2; tl++) {
+      std::stable_sort(part[tl].begin(), part[tl].end(), by_cost);
+      std::vector<Keyed> merged(full[tl].size() + part[tl].size());
+      std::merge(full[tl].begin(), full[tl].end(), part[tl].begin(), part[tl].end(),
+                 merged.begin(), by_cost);
+      for (const Keyed &k : merged)
+         B->items.push_back(k.it);
+   }
+   B->n_untilted = 0;
+   while (B->n_untilted < (int64_t)B->items.size() && !B->items[B->n_untilted].tilted)
+      B->n_untilted++;
+   B->shape = shape;
 }
 
 int plan_batch(int64_t n_tiles, const fpgb_volume *vols, const fpgb_fibers *fibers,
@@ -299,57 +387,16 @@ int plan_batch(int64_t n_tiles, const fpgb_volume *vols, const fpgb_fibers *fibe
       }
    }
 
-   // work items, most expensive first (rays x steps per ray) in two queues
-   // (untilted, then tilted: separate kernels), so that the dynamic queue
-   // balances well.  A pair's full 128-ray items all cost 128 n_z: the pairs
-   // are ordered by n_z and their full items emitted in that order, and the
-   // pairs' last, partial items are merged in by cost (no sort over the
-   // ~10^6 items of a large batch).
-   {
-      const int64_t R = B->rays_per_item;
-      std::vector<int32_t> order(B->pairs.size());
-      for (size_t p = 0; p < order.size(); p++)
-         order[p] = (int32_t)p;
-      auto tilted = [&](int32_t p) { return B->pairs[p].prm.tilted; };
-      auto nz = [&](int32_t p) { return (int64_t)B->pairs[p].prm.n_z; };
-      std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
-         if (tilted(a) != tilted(b))
-            return tilted(a) < tilted(b);
-         return nz(a) > nz(b);
-      });
-      struct Keyed {
-         int64_t cost;
-         BatchItem it;
-      };
-      std::vector<Keyed> full[2], part[2];
-      for (int32_t p : order) {
-         const MarchParams &M = B->pairs[p].prm;
-         const int64_t rays = M.X * M.Y;
-         const int tl = M.tilted ? 1 : 0;
-         for (int64_t r0 = 0; r0 < rays; r0 += R) {
-            BatchItem it{};
-            it.pair = p;
-            it.tilted = M.tilted;
-            it.ray_begin = r0;
-            it.ray_count = (int32_t)std::min<int64_t>(R, rays - r0);
-            (it.ray_count == R ? full : part)[tl].push_back({it.ray_count * nz(p), it});
-         }
-      }
-      auto by_cost = [](const Keyed &a, const Keyed &b) { return a.cost > b.cost; };
-      B->items.clear();
-      B->items.reserve(full[0].size() + full[1].size() + part[0].size() + part[1].size());
-      for (int tl = 0; tl < 2; tl++) {
-         std::stable_sort(part[tl].begin(), part[tl].end(), by_cost);
-         std::vector<Keyed> merged(full[tl].size() + part[tl].size());
-         std::merge(full[tl].begin(), full[tl].end(), part[tl].begin(), part[tl].end(),
-                    merged.begin(), by_cost);
-         for (const Keyed &k : merged)
-            B->items.push_back(k.it);
-      }
+   // the workspace holds the longest item list of any shape
+   for (int sh = 0; sh < kItemShapes; sh++) {
+      const int64_t tx = int64_t(1) << sh, ty = (int64_t)B->rays_per_item >> sh;
+      size_t n = 0;
+      for (const MarchPlan &mp : B->pairs)
+         n += sh == 0 ? (size_t)((mp.prm.X * mp.prm.Y + ty - 1) / ty)
+                      : (size_t)(((mp.prm.X + tx - 1) / tx) * ((mp.prm.Y + ty - 1) / ty));
+      B->max_items = std::max(B->max_items, n);
    }
-   B->n_untilted = 0;
-   while (B->n_untilted < (int64_t)B->items.size() && !B->items[B->n_untilted].tilted)
-      B->n_untilted++;
+   make_items(B, 0);
 
    // output arena: per tile label + vector, per pair image (+ epa)
    size_t a = 0;
@@ -373,7 +420,7 @@ int plan_batch(int64_t n_tiles, const fpgb_volume *vols, const fpgb_fibers *fibe
    B->ws_layers = take(w, sizeof(LayerDev) * B->layers.size());
    B->ws_tiles = take(w, sizeof(TileDev) * B->tile_dev.size() + 2 * sizeof(void *) * n_tiles);
    B->ws_prm = take(w, sizeof(MarchParams) * B->pairs.size());
-   B->ws_items = take(w, sizeof(BatchItem) * B->items.size());
+   B->ws_items = take(w, sizeof(BatchItem) * B->max_items);
    size_t tab = 0;
    for (const MarchPlan &mp : B->pairs) {
       B->table_off.push_back(tab);
@@ -516,9 +563,11 @@ int run_batch(fpgb_batch_impl *B, int march_ctas_per_sm, int chunk, int coop, cu
    const int ch = chunk > 0 ? chunk : 4;
 #define FPGB_BATCH_MARCH(M)                                                                    \
    FPGB_TRY((launch_batch_march<M, false>(prm, items, n0, next, counters, B->sms, B->fit[0],   \
-                                          march_ctas_per_sm, ch, coop, B->narrow, st)));            \
+                                          march_ctas_per_sm, ch, coop, B->narrow, B->shape,     \
+                                          st)));                                               \
    FPGB_TRY((launch_batch_march<M, true>(prm, items + n0, n1, next + 1, counters, B->sms,      \
-                                         B->fit[1], march_ctas_per_sm, ch, coop, B->narrow, st)))
+                                         B->fit[1], march_ctas_per_sm, ch, coop, B->narrow,    \
+                                         B->shape, st)))
    switch (B->setup.interpolate) {
    case 0: FPGB_BATCH_MARCH(0); break;
    case 1: FPGB_BATCH_MARCH(1); break;
@@ -628,6 +677,24 @@ int fpgb_batch_run(fpgb_batch *b, int march_ctas_per_sm, int items_per_grab, int
       return FPGB_EINVAL;
    }
    return run_batch(b, march_ctas_per_sm, items_per_grab, march_coop, as_stream(stream));
+}
+
+int fpgb_batch_set_shape(fpgb_batch *b, int shape, void *stream) {
+   if (!b || shape < 0 || shape >= kItemShapes) {
+      set_error("batch: null handle or ray-block shape not in 0..%d", kItemShapes - 1);
+      return FPGB_EINVAL;
+   }
+   if (shape == b->shape)
+      return FPGB_OK;
+   make_items(b, shape);
+   if (b->ws) { // bound: replace the device's item list
+      cudaStream_t st = as_stream(stream);
+      FPGB_CUDA_TRY(cudaMemcpyAsync(b->ws + b->ws_items, b->items.data(),
+                                    sizeof(BatchItem) * b->items.size(), cudaMemcpyHostToDevice,
+                                    st));
+      FPGB_CUDA_TRY(cudaStreamSynchronize(st)); // the host list may change again
+   }
+   return FPGB_OK;
 }
 
 int fpgb_batch_run_stages(fpgb_batch *b, int stages, int march_ctas_per_sm, int items_per_grab,

@@ -40,30 +40,41 @@ FPGB_HD void closest_point(const SegDev &S, const double pt[3],
 }
 
 // FP32 estimate of a candidate's dist^2 from segment-local inputs (w = voxel
-// centre - float(p - base), float(v), float(c2), float(1 / c2)), and a
-// bound: the float that
-// the reference's double arithmetic produces (exact_dist) lies in
-// [d2f - margin, d2f + margin].  The bound covers the rounding of the float
-// inputs, of every FP32 operation (written as fused multiply-adds: one
-// rounding each, the same on the host and the device), of the branch
-// decision (the distance is continuous across the branches) and of the
-// reference's own final rounding; a host build checks it over every voxel of
-// random segment boxes.
+// centre - float(p - base), float(v), float(c2), float(1 / c2)), and a bound:
+// the float that the reference's double arithmetic produces (exact_dist)
+// lies in [d2f - margin, d2f + margin].
+//
+// The estimate is |w - t v|^2 = w.w - 2 t (w.v) + t^2 (v.v) at t = clamp(w.v /
+// v.v, 0, 1) — the closest-point parameter, so no branch: for t = 0 it is
+// |w|^2, for t = 1 |w - v|^2, in between |w|^2 - (w.v)^2 / v.v.  An error in
+// t only raises the value by v.v (dt)^2 (the expression is the squared
+// distance to a point of the segment, minimal at the exact t).  The y and z
+// parts of w.w and w.v are passed in (a = wy vy + wz vz, b = wy^2 + wz^2):
+// the voxelizer's sweep computes them once per (y, z) cell and visits the x
+// of the cell's column, so the per-candidate work is six fused operations.
+// The bound covers the rounding of the float inputs, of every FP32 operation
+// (fused multiply-adds: one rounding each, the same on the host and the
+// device) and of the reference's own final rounding; a host build checks it
+// over every voxel of random segment boxes (tests/test_voxel_fastpath.py).
+FPGB_HD float dist2_yz_dot(float wy, float wz, float vy, float vz) {
+   return fmaf(wz, vz, wy * vy);
+}
+FPGB_HD float dist2_yz_len(float wy, float wz) { return fmaf(wz, wz, wy * wy); }
+
+FPGB_HD float approx_dist2_x(float wx, float a, float b, float vx, float c2f, float rc2,
+                             float &margin) {
+   const float c1 = fmaf(wx, vx, a);
+   const float w2 = fmaf(wx, wx, b);
+   const float t = fminf(fmaxf(c1 * rc2, 0.f), 1.f);
+   const float m = fmaf(t, c2f, -2.f * c1);
+   margin = fmaf(3.8e-6f, w2 + c2f, 1e-4f);
+   return fmaf(t, m, w2);
+}
+
 FPGB_HD float approx_dist2(float wx, float wy, float wz, float vx, float vy, float vz,
                            float c2f, float rc2, float &margin) {
-   const float c1f = fmaf(wz, vz, fmaf(wy, vy, wx * vx));
-   const float w2 = fmaf(wz, wz, fmaf(wy, wy, wx * wx));
-   float d2f;
-   if (c1f <= 0.f) {
-      d2f = w2;
-   } else if (c1f >= c2f) {
-      const float ux = wx - vx, uy = wy - vy, uz = wz - vz;
-      d2f = fmaf(uz, uz, fmaf(uy, uy, ux * ux));
-   } else {
-      d2f = fmaf(-c1f, c1f * rc2, w2);
-   }
-   margin = fmaf(3.8e-6f, w2 + c2f, 1e-4f);
-   return d2f;
+   return approx_dist2_x(wx, dist2_yz_dot(wy, wz, vy, vz), dist2_yz_len(wy, wz), vx, c2f, rc2,
+                         margin);
 }
 
 // float(|cl - pt|^2) and float(r(t)^2) exactly as generator.cpp:327-328.

@@ -155,10 +155,13 @@ __device__ __forceinline__ SegSweep load_sweep(const SegDev &S) {
 }
 
 // The part of segment S's clipped box inside the brick (origin o, extent n),
-// walked by a warp 32 voxels at a time in a flattened (x, y, z) order.
+// swept as columns along x: its ey x ez (y, z) cells are numbered z fastest,
+// lane l of chunk c owns cell 32 c + l and visits the ex voxels of that
+// cell's x column.  The y and z parts of the estimate are computed once per
+// cell; each voxel then costs six fused operations (approx_dist2_x).
 struct SubBox {
-   int x0, y0, z0, ey, ez, n;
-   float inv_ez, inv_eyz; // 1/ez, 1/(ey*ez) for division-free index splits
+   int x0, y0, z0, ex, ey, ez, ncell;
+   float inv_ez; // 1/ez for the division-free cell split
 };
 
 __device__ __forceinline__ bool sub_box(const SegSweep &w, int ox, int oy, int oz, int nx,
@@ -166,27 +169,14 @@ __device__ __forceinline__ bool sub_box(const SegSweep &w, int ox, int oy, int o
    b.x0 = max(w.d.y, ox);
    b.y0 = max(w.d.z, oy);
    b.z0 = max(w.d.w, oz);
-   const int ex = min(w.d.y + w.e.x, ox + nx) - b.x0;
+   b.ex = min(w.d.y + w.e.x, ox + nx) - b.x0;
    b.ey = min(w.d.z + w.e.y, oy + ny) - b.y0;
    b.ez = min(w.d.w + w.e.z, oz + nz) - b.z0;
-   if (ex <= 0 || b.ey <= 0 || b.ez <= 0)
+   if (b.ex <= 0 || b.ey <= 0 || b.ez <= 0)
       return false;
-   b.n = ex * b.ey * b.ez;
+   b.ncell = b.ey * b.ez;
    b.inv_ez = __frcp_rn((float)b.ez);
-   b.inv_eyz = __frcp_rn((float)(b.ey * b.ez));
    return true;
-}
-
-// k-th voxel of the sub-box.  (k + 1/2) / e lies at least 1/(2e) >= 2^-9
-// from an integer for k < 2048 and e <= 256, far beyond the float error of
-// the product, so the truncations are the exact integer quotients.
-__device__ __forceinline__ void sub_box_voxel(const SubBox &b, int k, int &x, int &y, int &z) {
-   const int ix = (int)(((float)k + 0.5f) * b.inv_eyz);
-   const int r = k - ix * (b.ey * b.ez);
-   const int iy = (int)(((float)r + 0.5f) * b.inv_ez);
-   x = b.x0 + ix;
-   y = b.y0 + iy;
-   z = b.z0 + (r - iy * b.ez);
 }
 
 __device__ __forceinline__ int brick_index(int x, int y, int z, int ox, int oy, int oz) {
@@ -204,90 +194,59 @@ __device__ __forceinline__ SegFP32 seg_fp32(const SegSweep &w) {
                   __float_as_int(w.c.z), __float_as_int(w.c.w), w.d.x};
 }
 
-// Lane-dense walk over a sub-box: lane l visits the voxels k = l, l + 32,
-// l + 64, ... of the flattened (x, y, z) order.  The position advances by 32
-// with mixed-radix carries (z into y, y into x; one carry each at most, since
-// the step's z and y parts are below ez and ey), and the brick index and the
-// float offsets (x - base) + 1/2 — half-integers, exact in float — advance
-// with it, so the sweep does no division or int/float conversion per voxel.
-struct BoxWalk {
-   int k, n, li, dli, cz, cy;
-   float gx, gy, gz, dgx, dgy, dgz, gz_end, gy_end, fez, fey;
+// A lane's (y, z) cell of a chunk: its brick index at x = x0, and the y / z
+// parts of the estimate.  (c + 1/2) / ez lies at least 1/(2 ez) >= 2^-6 from
+// an integer for c < 256 and ez <= 32, far beyond the float error of the
+// product, so the truncation is the exact quotient.
+struct Cell {
+   int li;
+   float a, b;
 };
 
-__device__ __forceinline__ BoxWalk box_walk(const SubBox &b, const SegFP32 &g, int ox, int oy,
-                                            int oz, int lane) {
-   BoxWalk w;
-   int x, y, z, sx, sy, sz;
-   sub_box_voxel(b, lane, x, y, z);
-   sub_box_voxel(b, 32, sx, sy, sz); // voxel 32 relative to voxel 0: the step
-   sx -= b.x0;
-   sy -= b.y0;
-   sz -= b.z0;
-   w.k = lane;
-   w.n = b.n;
-   w.li = brick_index(x, y, z, ox, oy, oz);
-   w.dli = (sx * kBrickY + sy) * kBrickZ + sz;
-   w.cz = kBrickZ - b.ez;             // z carry: z -= ez, y += 1
-   w.cy = (kBrickY - b.ey) * kBrickZ; // y carry: y -= ey, x += 1
-   w.gx = (float)(x - g.bx) + 0.5f;
-   w.gy = (float)(y - g.by) + 0.5f;
-   w.gz = (float)(z - g.bz) + 0.5f;
-   w.dgx = (float)sx;
-   w.dgy = (float)sy;
-   w.dgz = (float)sz;
-   w.gz_end = (float)(b.z0 + b.ez - g.bz) + 0.5f;
-   w.gy_end = (float)(b.y0 + b.ey - g.by) + 0.5f;
-   w.fez = (float)b.ez;
-   w.fey = (float)b.ey;
-   return w;
+__device__ __forceinline__ Cell cell_of(const SubBox &b, const SegFP32 &g, int c, int ox, int oy,
+                                        int oz) {
+   const int iy = (int)(((float)c + 0.5f) * b.inv_ez);
+   const int y = b.y0 + iy, z = b.z0 + (c - iy * b.ez);
+   // voxel centre - float(p - base): (y - base) + 1/2 is exact in float
+   const float wy = ((float)(y - g.by) + 0.5f) - g.pfy;
+   const float wz = ((float)(z - g.bz) + 0.5f) - g.pfz;
+   return Cell{brick_index(b.x0, y, z, ox, oy, oz), dist2_yz_dot(wy, wz, g.vy, g.vz),
+               dist2_yz_len(wy, wz)};
 }
 
-__device__ __forceinline__ void box_step(BoxWalk &w) {
-   w.k += 32;
-   w.li += w.dli;
-   w.gx += w.dgx;
-   w.gy += w.dgy;
-   w.gz += w.dgz;
-   if (w.gz >= w.gz_end) {
-      w.gz -= w.fez;
-      w.gy += 1.f;
-      w.li += w.cz;
-   }
-   if (w.gy >= w.gy_end) {
-      w.gy -= w.fey;
-      w.gx += 1.f;
-      w.li += w.cy;
-   }
-}
-
-// FP32 estimate of the candidate (segment, voxel at offsets g* from the
-// segment's base): its dist^2 lies in [lo, hi] (directed rounding of
-// estimate -/+ bound).
-__device__ __forceinline__ void candidate_bounds(const SegFP32 &g, float gx, float gy, float gz,
+// FP32 estimate of the candidate at x offset gx = (x - base) + 1/2 of a
+// cell: its dist^2 lies in [lo, hi] (directed rounding of estimate -/+
+// bound).
+__device__ __forceinline__ void candidate_bounds(const SegFP32 &g, const Cell &c, float gx,
                                                  float &lo, float &hi) {
    float mg;
-   const float d2f = approx_dist2(gx - g.pfx, gy - g.pfy, gz - g.pfz, g.vx, g.vy, g.vz, g.c2f,
-                                  g.rc2, mg);
+   const float d2f = approx_dist2_x(gx - g.pfx, c.a, c.b, g.vx, g.c2f, g.rc2, mg);
    lo = __fsub_rd(d2f, mg);
    hi = __fadd_ru(d2f, mg);
 }
 
-// BOUND pass of one segment over its sub-box.
+// BOUND pass of one segment over its sub-box: the upper bound of every
+// certainly accepted candidate goes to the voxel's 32-bit bound (a float
+// >= 0, so its bits order like the value).  Lanes take cells independently.
 template <bool MULTI>
 __device__ __forceinline__ void brick_bound(const SegSweep &sw, const SubBox &b, int ox, int oy,
-                                            int oz, unsigned long long *skey, unsigned *sminb,
-                                            int lane) {
+                                            int oz, unsigned *sub, unsigned *sminb, int lane) {
    const SegFP32 g = seg_fp32(sw);
    const unsigned bundle = (unsigned)sw.e.w;
-   for (BoxWalk w = box_walk(b, g, ox, oy, oz, lane); w.k < w.n; box_step(w)) {
-      float lo, hi;
-      candidate_bounds(g, w.gx, w.gy, w.gz, lo, hi);
-      if (!(hi <= g.acc))
-         continue;
-      atomicMin(&skey[w.li], ((unsigned long long)__float_as_uint(hi) << 32) | 0xFFFFFFFFull);
-      if (MULTI)
-         atomicMin(&sminb[w.li], bundle);
+   const float gx0 = (float)(b.x0 - g.bx) + 0.5f;
+   for (int c0 = lane; c0 < b.ncell; c0 += 32) {
+      const Cell c = cell_of(b, g, c0, ox, oy, oz);
+      float gx = gx0;
+      int li = c.li;
+      for (int i = 0; i < b.ex; i++, gx += 1.f, li += kBrickY * kBrickZ) {
+         float lo, hi;
+         candidate_bounds(g, c, gx, lo, hi);
+         if (hi <= g.acc) {
+            atomicMin(&sub[li], __float_as_uint(hi));
+            if (MULTI)
+               atomicMin(&sminb[li], bundle);
+         }
+      }
    }
 }
 
@@ -391,40 +350,45 @@ __device__ __forceinline__ void brick_filter(const SegSweep &sw, unsigned slot, 
                                              const LayerDev *__restrict__ layers, int layer_base,
                                              unsigned *sminb, unsigned long long &n_slow) {
    const SegFP32 g = seg_fp32(sw);
-   BoxWalk w = box_walk(b, g, ox, oy, oz, lane);
-   for (int k0 = 0; k0 < b.n; k0 += 32, box_step(w)) {
-      bool need = false;
-      unsigned short e = 0;
-      if (w.k < w.n) {
-         float lo, hi;
-         candidate_bounds(g, w.gx, w.gy, w.gz, lo, hi);
-         if (!(lo > g.thr)) { // inside the outermost layer at the thickest end
-            const bool certain = hi <= g.acc;
-            const int li = w.li;
-            // keys only decrease, so any value read bounds the final one from
-            // above; the initial ~0 reads as NaN and skips nothing
-            const unsigned long long cur =
-                *reinterpret_cast<volatile unsigned long long *>(&skey[li]);
-            const bool loser = lo > __uint_as_float((unsigned)(cur >> 32));
-            need = !(loser && (certain || !MULTI));
-            e = (unsigned short)(li | (certain ? kQueueCertain : 0) |
-                                 (loser ? kQueueBundleOnly : 0));
+   const float gx0 = (float)(b.x0 - g.bx) + 0.5f;
+   for (int c0 = 0; c0 < b.ncell; c0 += 32) { // whole warps: the queue is filled by ballot
+      const bool in = c0 + lane < b.ncell;
+      const Cell c = cell_of(b, g, in ? c0 + lane : 0, ox, oy, oz);
+      float gx = gx0;
+      int li = c.li;
+      for (int i = 0; i < b.ex; i++, gx += 1.f, li += kBrickY * kBrickZ) {
+         bool need = false;
+         unsigned short e = 0;
+         if (in) {
+            float lo, hi;
+            candidate_bounds(g, c, gx, lo, hi);
+            if (!(lo > g.thr)) { // inside the outermost layer at the thickest end
+               const bool certain = hi <= g.acc;
+               // keys only decrease, so any value read bounds the final one
+               // from above; the initial ~0 reads as NaN and skips nothing
+               const unsigned long long cur =
+                   *reinterpret_cast<volatile unsigned long long *>(&skey[li]);
+               const bool loser = lo > __uint_as_float((unsigned)(cur >> 32));
+               need = !(loser && (certain || !MULTI));
+               e = (unsigned short)(li | (certain ? kQueueCertain : 0) |
+                                    (loser ? kQueueBundleOnly : 0));
+            }
          }
-      }
-      const unsigned m = __ballot_sync(0xFFFFFFFFu, need);
-      if (need) {
-         const int at = qn + __popc(m & ((1u << lane) - 1u));
-         q.slot[at] = slot;
-         q.entry[at] = e;
-      }
-      qn += __popc(m);
-      if (qn >= 32) { // drain 32 entries with every lane
-         __syncwarp();
-         const int at = qn - 32 + lane;
-         brick_eval<MULTI>(segs, list, layers, layer_base, q.slot[at], q.entry[at], ox, oy, oz,
-                           skey, sminb, n_slow);
-         qn -= 32;
-         __syncwarp();
+         const unsigned m = __ballot_sync(0xFFFFFFFFu, need);
+         if (need) {
+            const int at = qn + __popc(m & ((1u << lane) - 1u));
+            q.slot[at] = slot;
+            q.entry[at] = e;
+         }
+         qn += __popc(m);
+         if (qn >= 32) { // drain 32 entries with every lane
+            __syncwarp();
+            const int at = qn - 32 + lane;
+            brick_eval<MULTI>(segs, list, layers, layer_base, q.slot[at], q.entry[at], ox, oy,
+                              oz, skey, sminb, n_slow);
+            qn -= 32;
+            __syncwarp();
+         }
       }
    }
 }
@@ -505,11 +469,13 @@ voxel_bricks(const SegDev *__restrict__ segs, const TileDev *__restrict__ tiles,
              int32_t *const *__restrict__ labels, float *const *__restrict__ vecs,
              unsigned long long *__restrict__ counters) {
    __shared__ unsigned long long skey[kBrickVoxels];
+   __shared__ unsigned sub[kBrickVoxels]; // BOUND pass: upper bound of the winner's dist^2
    __shared__ unsigned sminb[MULTI ? kBrickVoxels : 1];
    __shared__ WarpQueue queues[kBrickWarps];
    __shared__ unsigned s_next[2]; // next segment of the brick's list, per pass
    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
    unsigned long long n_slow = 0, n_overlap = 0, n_overflow = 0;
+
    for (int64_t brick = brick_begin + blockIdx.x; brick < brick_end; brick += gridDim.x) {
       // tile of the brick: last tile whose brick_base <= brick
       int64_t lo = 0, hi = n_tiles - 1;
@@ -531,15 +497,15 @@ voxel_bricks(const SegDev *__restrict__ segs, const TileDev *__restrict__ tiles,
       const int layer_base = T.layer_base, max_layer = T.max_layer;
 
       for (int i = threadIdx.x; i < kBrickVoxels; i += kBrickThreads) {
-         skey[i] = ~0ull;
+         sub[i] = ~0u;
          if (MULTI)
             sminb[i] = ~0u;
       }
+      // (clamped to the planned list size: every slot below it is written)
+      const unsigned j1 = min(offsets[brick + 1], n_pairs), j0 = min(offsets[brick], j1);
       if (threadIdx.x < 2)
          s_next[threadIdx.x] = 0;
       __syncthreads();
-      // (clamped to the planned list size: every slot below it is written)
-      const unsigned j1 = min(offsets[brick + 1], n_pairs), j0 = min(offsets[brick], j1);
       // BOUND pass: warps take segments from a shared counter
       for (;;) {
          unsigned j = 0;
@@ -551,10 +517,15 @@ voxel_bricks(const SegDev *__restrict__ segs, const TileDev *__restrict__ tiles,
          const SegSweep sw = load_sweep(segs[list[j]]);
          SubBox b;
          if (sub_box(sw, ox, oy, oz, nx, ny, nz, b))
-            brick_bound<MULTI>(sw, b, ox, oy, oz, skey, sminb, lane);
+            brick_bound<MULTI>(sw, b, ox, oy, oz, sub, sminb, lane);
       }
       __syncthreads();
-      // EXACT pass
+      // the bounds become the keys ub << 32 | 0xFFFFFFFF the EXACT pass
+      // filters against and lowers (no bound: ~0, which reads as NaN)
+      for (int i = threadIdx.x; i < kBrickVoxels; i += kBrickThreads)
+         skey[i] = sub[i] == ~0u ? ~0ull : ((unsigned long long)sub[i] << 32) | 0xFFFFFFFFull;
+      __syncthreads();
+      // EXACT pass: warps take segments from a shared counter again
       {
          WarpQueue &q = queues[warp];
          int qn = 0;

@@ -101,14 +101,16 @@ class GpuRunner:
                                        voxel_size=r.tile.voxel_size, bundles=r.tile.bundles,
                                        layers=r.tile.layers, tilts=r.tilts) for r in reqs]
         b = TileBatch(tiles, self.setup, epa=True)
+        if self.tune:
+            from . import autotune
+            cache = autotune._load()
+            k = autotune.key(b)
+            if k in cache:
+                b.config = tuple(cache[k]["config"])
+                if len(b.config) > 3:
+                    b.set_shape(b.config[3])  # before the upload: no extra copy
         with torch.cuda.stream(stream):
             b.allocate(stream=stream)
-            if self.tune:
-                from . import autotune
-                cache = autotune._load()
-                k = autotune.key(b)
-                if k in cache:
-                    b.config = tuple(cache[k]["config"])
             b.run(stream=stream)
             ev = torch.cuda.Event()
             ev.record(stream)

@@ -87,8 +87,15 @@ def test_batch_bit_identical_to_single_volume_path(cuda, coop, wide, monkeypatch
             ref = sim.run_simulation(tile.dim, lab, vec, props, th, ph)
             assert np.array_equal(b.image(p).cpu().numpy(), ref), f"tile {t} pair {p}"
     assert w["fp64_replays"] >= 0
-    # a CUDA-graph replay reproduces the run exactly
+    # every ray-block shape of the march gives the same bits
     before = [b.image(p).clone() for p in range(int(b.info.n_pairs))]
+    for shape in (1, 2, 3):
+        b.run(shape=shape)
+        torch.cuda.synchronize()
+        for p in range(int(b.info.n_pairs)):
+            assert torch.equal(b.image(p), before[p]), (shape, p)
+    b.set_shape(0)
+    # a CUDA-graph replay reproduces the run exactly
     b.arena.zero_()
     b.replay()
     torch.cuda.synchronize()
@@ -108,7 +115,8 @@ def test_autotune_picks_a_config_and_results_do_not_change(cuda, tmp_path, monke
     torch.cuda.synchronize()
     ref = [b.image(p).clone() for p in range(int(b.info.n_pairs))]
     cfg, ms, table = autotune.tune(b, reps=1)
-    assert cfg in table and ms > 0
+    assert cfg in table and ms > 0 and len(cfg) == 4
+    assert {c[3] for c in table} == set(autotune.SHAPES)  # every ray-block shape was timed
     b.run()
     torch.cuda.synchronize()
     for p in range(int(b.info.n_pairs)):
