@@ -263,11 +263,21 @@ class ForwardServer:
 
 
 def latency_stats(reqs):
-    lat = np.array([r.latency for r in reqs if r.latency is not None and r.error is None])
+    """p50 / p99 / mean arrival-to-result latency of the completed requests,
+    and its two parts: waiting for admission (arrival to launch) and service
+    (launch to result on the host)."""
+    ok = [r for r in reqs if r.latency is not None and r.error is None]
+    lat = np.array([r.latency for r in ok])
     if lat.size == 0:
         return {"n": 0}
-    return {"n": int(lat.size), "p50_ms": float(np.percentile(lat, 50) * 1e3),
-            "p99_ms": float(np.percentile(lat, 99) * 1e3), "mean_ms": float(lat.mean() * 1e3)}
+    wait = np.array([r.t_start - r.arrival for r in ok if r.t_start is not None])
+    serv = np.array([r.t_done - r.t_start for r in ok if r.t_start is not None])
+    out = {"n": int(lat.size), "p50_ms": float(np.percentile(lat, 50) * 1e3),
+           "p99_ms": float(np.percentile(lat, 99) * 1e3), "mean_ms": float(lat.mean() * 1e3)}
+    if wait.size:
+        out.update(wait_p50_ms=float(np.percentile(wait, 50) * 1e3),
+                   service_p50_ms=float(np.percentile(serv, 50) * 1e3))
+    return out
 
 
 class PlainRunner:
