@@ -62,6 +62,9 @@ CPU_SAMPLE_STRIDE = 8      # GPU arm's CPU baseline / parity: every 8th tile (32
 REF_TILES_PER_STEP = 8     # reference arm: 8 consecutive tiles per step, rotating
 VOXELIZER_LAUNCHES = 4     # brick_bin (count), brick_scan, brick_bin (fill), voxel_bricks
 MARCH_LAUNCHES = 2         # batch_march untilted, tilted
+# units of the committed ncu captures (profiles/*_tiles16.md): the first 16 tiles
+PROFILED_TILTED_STEPS = 268946100   # batch_march, tilted launch
+PROFILED_VOXELS = 67210825          # voxel_bricks
 
 
 def _dist_env():
@@ -466,18 +469,31 @@ def run_gpu(args):
     vox_bytes = 16 * vox
     march_gbs = march_bytes / (march_ms * 1e-3) / 1e9
     vox_gbs = vox_bytes / (vox_ms * 1e-3) / 1e9
+    # DRAM traffic from the committed ncu captures of the same kernels on the
+    # first 16 tiles (a --set full capture of the whole batch is too large),
+    # scaled to this batch by the units processed: the tilted march by its
+    # steps (the untilted column march reads each voxel once per tilt: 16 B a
+    # step), the voxelizer by its voxels
+    import oracle
+    tilted = sum(oracle.count_steps(t.dim, th, t.setup_kwargs()["step_size"])
+                 for t in tiles for th, _ in t.tilts if float(th) != 0.0)
     if march_ms >= vox_ms:
-        prof = "batch_march_tiles256.md"
+        prof = "batch_march_tiles16.md"
+        t16 = _ncu_traffic(prof)
+        traffic = (None if t16 is None
+                   else t16 * tilted / PROFILED_TILTED_STEPS + 16.0 * (steps - tilted))
         roof = {"kernel": "batch_march (2 launches: untilted, tilted)", "bound": "hbm",
                 "achieved": march_gbs, "peak": hbm, "unit": "GB/s", "frac": march_gbs / hbm,
-                "traffic": _ncu_traffic(prof), "traffic_per": "batch (ncu)",
+                "traffic": traffic, "traffic_per": "batch: ncu of 16 tiles scaled by steps",
                 "limiter": _ncu_limiter(prof), "algorithmic_bytes_per_launch": march_bytes,
                 "algorithmic_bytes_per_step": 16, "peak_source": peak_kind}
     else:
-        prof = "voxel_bricks_tiles256.md"
+        prof = "voxel_bricks_tiles16.md"
+        t16 = _ncu_traffic(prof)
         roof = {"kernel": "voxel_bricks (+ binning)", "bound": "hbm", "achieved": vox_gbs,
                 "peak": hbm, "unit": "GB/s", "frac": vox_gbs / hbm,
-                "traffic": _ncu_traffic(prof), "traffic_per": "one launch (ncu)",
+                "traffic": None if t16 is None else t16 * vox / PROFILED_VOXELS,
+                "traffic_per": "one launch: ncu of 16 tiles scaled by voxels",
                 "limiter": _ncu_limiter(prof), "algorithmic_bytes_per_launch": vox_bytes,
                 "algorithmic_bytes_per_voxel": 16, "peak_source": peak_kind}
     cands = candidate_tests(tiles)
