@@ -71,6 +71,7 @@ _SIGS = {
     "fpgb_last_error": ([], ctypes.c_char_p),
     "fpgb_version": ([], ctypes.c_char_p),
     "fpgb_release_pool": ([], ctypes.c_int),
+    "fpgb_release_thread_pool": ([], ctypes.c_int),
     "fpgb_generate_tissue": ([_P, _P, ctypes.c_int, _P, _P, _P, _I64, _P, _P],
                              ctypes.c_int),
     "fpgb_generate_workspace_size": ([_P, _P], ctypes.c_size_t),

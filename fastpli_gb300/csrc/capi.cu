@@ -136,6 +136,29 @@ int pool_release_all() {
    return FPGB_OK;
 }
 
+int pool_release_thread() {
+   int dev = 0;
+   FPGB_CUDA_TRY(cudaGetDevice(&dev));
+   const std::thread::id me = std::this_thread::get_id();
+   std::lock_guard<std::mutex> lk(g_pool_mu);
+   bool any = false;
+   for (const auto &kv : g_pool)
+      any = any || (kv.first.dev == dev && kv.first.thread == me && kv.second.ptr);
+   if (!any)
+      return FPGB_OK;
+   FPGB_CUDA_TRY(cudaDeviceSynchronize()); // this thread's queued work may still use them
+   for (auto it = g_pool.begin(); it != g_pool.end();) {
+      if (it->first.dev == dev && it->first.thread == me) {
+         if (it->second.ptr)
+            FPGB_CUDA_TRY(cudaFree(it->second.ptr));
+         it = g_pool.erase(it);
+      } else {
+         ++it;
+      }
+   }
+   return FPGB_OK;
+}
+
 int warnings_from_counters(const long long *h, fpgb_warnings *w) {
    if (!w)
       return FPGB_OK;
@@ -157,5 +180,7 @@ const char *fpgb_last_error(void) { return fpgb::g_last_error.c_str(); }
 const char *fpgb_version(void) { return "fastpli_gb300 0.1.0 (sm_103a)"; }
 
 int fpgb_release_pool(void) { return fpgb::pool_release_all(); }
+
+int fpgb_release_thread_pool(void) { return fpgb::pool_release_thread(); }
 
 } // extern "C"

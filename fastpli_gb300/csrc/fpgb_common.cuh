@@ -69,6 +69,9 @@ enum PoolSlot : int {
 // buffer of the device and must not overlap other calls of the library.
 int pool_get(int slot, size_t bytes, void **ptr, cudaStream_t stream = nullptr);
 int pool_release_all();
+// Frees the calling thread's buffers on the current device (after
+// synchronising it): for threads that end, e.g. a server's worker.
+int pool_release_thread();
 
 // Touch one byte of every page of a host output buffer from several threads,
 // so that the device-to-host copy that follows finds its pages mapped.  A

@@ -228,6 +228,15 @@ class ForwardServer:
         self._inflight = still
 
     def _loop(self):
+        try:
+            self._serve()
+        finally:
+            if self._streams and not isinstance(self._streams[0], str):
+                # the library's cached buffers of this worker thread
+                from . import _native
+                _native.load().fpgb_release_thread_pool()
+
+    def _serve(self):
         while True:
             with self._lock:
                 if not self._run and not self._pending and not self._inflight:

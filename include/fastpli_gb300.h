@@ -259,6 +259,13 @@ int fpgb_rofl_device(const double *d_data, int64_t n_pix, int64_t n_rot, double 
  * run while another thread is inside a call of this library. */
 int fpgb_release_pool(void);
 
+/* Release the buffers the calling host thread holds in that pool on the
+ * current device (synchronises the device first).  A thread that has made
+ * its last call of this library, e.g. a serving worker about to end, frees
+ * its share without touching other threads' buffers.  No counterpart in the
+ * reference (whose calls allocate and free host memory per call). */
+int fpgb_release_thread_pool(void);
+
 #ifdef __cplusplus
 }
 #endif
