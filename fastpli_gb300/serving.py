@@ -138,9 +138,10 @@ class ForwardServer:
         self.budget = float(hbm_budget)
         self.max_tiles = int(max_tiles)
         self.runner = runner if runner is not None else GpuRunner(setup)
-        # batches of one request: the plain per-call path (same results)
+        # batches of one request: the single-volume kernels, the request's
+        # tilts overlapped on the library's streams (same results)
         self.single = single_runner if single_runner is not None else (
-            PlainRunner(setup) if runner is None else None)
+            PlainRunner(setup, overlap_tilts=True) if runner is None else None)
         self.n_rho = self.runner.n_rho
         self._streams = streams
         self.n_slots = int(n_slots)
@@ -292,11 +293,16 @@ def latency_stats(reqs):
 class PlainRunner:
     """The plain per-call path as a runner (one request at a time): voxelize
     with ``_Generator.run_generation_device``, then one
-    ``_Simulator.run_simulation_device(epa=True)`` per tilt.  Used as the
-    baseline the batched server is compared with."""
+    ``_Simulator.run_simulation_device(epa=True)`` per tilt, each tilt's
+    maps copied to the host on their own.  Used as the baseline the batched
+    server is compared with.  With ``overlap_tilts`` (the batched server's
+    path for a lone request) the tilts run through ``run_tilts_device`` on
+    the library's streams and all maps come back in one copy; the results
+    are the same bits."""
 
-    def __init__(self, setup):
+    def __init__(self, setup, overlap_tilts=False):
         from .simulation import _Simulator
+        self.overlap_tilts = bool(overlap_tilts)
         self.setup = dict(setup)
         self.n_rho = len(np.asarray(setup["filter_rotations"]).reshape(-1))
         self.sim = _Simulator()
@@ -317,6 +323,11 @@ class PlainRunner:
                 g.set_volume(r.tile.dim, r.tile.origin, r.tile.voxel_size)
                 g.set_fiber_bundles(r.tile.bundles, r.tile.layers)
                 lab, vec, props, _ = g.run_generation_device(stream=stream, sync_warnings=False)
+                if self.overlap_tilts:
+                    res = self.sim.run_tilts_device(r.tile.dim, lab, vec, props, r.tilts,
+                                                    epa=True, stream=stream, sync_warnings=False)
+                    out.append(torch.stack([torch.stack(x[1:]) for x in res]))  # [k, 3, X, Y]
+                    continue
                 maps = [self.sim.run_simulation_device(r.tile.dim, lab, vec, props, float(t),
                                                        float(p), epa=True, stream=stream,
                                                        sync_warnings=False)[1:]
@@ -328,5 +339,9 @@ class PlainRunner:
 
     def collect(self, h, reqs, stream):
         for maps, r in zip(h, reqs):
-            r.result = {"epa": [tuple(m.cpu().numpy() for m in tdr) for tdr in maps],
-                        "images": None}
+            if isinstance(maps, list):
+                epa = [tuple(m.cpu().numpy() for m in tdr) for tdr in maps]
+            else:  # one block of every tilt's maps: one copy
+                a = maps.cpu().numpy()
+                epa = [(a[i, 0], a[i, 1], a[i, 2]) for i in range(a.shape[0])]
+            r.result = {"epa": epa, "images": None}
