@@ -248,6 +248,11 @@ class TileBatch:
         with torch.cuda.stream(st):
             out[:nbytes].copy_(self.arena[lo: lo + nbytes], non_blocking=True)
         st.synchronize()
+        return out, self.host_views(out)
+
+    def host_views(self, out):
+        """Per-pair numpy image views into a host copy of the output region."""
+        lo = int(self.image_off[0])
         base = out.numpy()
         views = []
         for p in range(int(self.info.n_pairs)):
@@ -255,7 +260,7 @@ class TileBatch:
             o = int(self.image_off[p]) - lo
             views.append(base[o: o + 8 * X * Y * self.n_rho].view(np.float64)
                          .reshape(X, Y, self.n_rho))
-        return out, views
+        return views
 
     @property
     def output_bytes(self):
@@ -282,6 +287,71 @@ class TileBatch:
             self.close()
         except Exception:
             pass
+
+
+def run_tiles_host(tiles, setup, chunks=4, config=None, flat_fibers=None, host_buffers=None):
+    """The forward model of many tiles from host fibers to host images,
+    pipelined: the tiles are cut into ``chunks`` contiguous groups of about
+    equal voxel count; while the GPU voxelizes and marches group c, a host
+    thread plans group c + 1 (``fpgb_batch_create`` releases the GIL), and
+    group c's images go down on a copy stream while group c + 1 runs.
+    Returns (images, stats): one float64 [X, Y, n_rho] numpy array per
+    (tile, tilt) pair in tile order, views into page-locked buffers (pass
+    the ``host_buffers`` list of an earlier call to reuse them), and the bytes
+    moved each way.  ``config`` is the march configuration (``TileBatch.config``,
+    e.g. from ``autotune``).  Each image is the one the single-volume path
+    gives for that tile and tilt."""
+    import concurrent.futures as cf
+    import torch
+    tiles = list(tiles)
+    flats = list(flat_fibers) if flat_fibers is not None else flatten(tiles)
+    vox = np.array([float(np.prod(t.dim)) for t in tiles])
+    cut = np.searchsorted(np.cumsum(vox), vox.sum() * np.arange(1, chunks) / chunks)
+    bounds = [0] + sorted(set(int(c) + 1 for c in cut if 0 <= c < len(tiles) - 1)) + [len(tiles)]
+    groups = [list(range(a, b)) for a, b in zip(bounds[:-1], bounds[1:]) if b > a]
+    comp = torch.cuda.current_stream()
+    up = torch.cuda.Stream()
+    down = torch.cuda.Stream()
+    host = list(host_buffers) if host_buffers is not None else []
+    batches, images, h2d, d2h = [], [], 0, 0
+
+    def plan(g):
+        b = TileBatch([tiles[i] for i in g], setup, flat_fibers=[flats[i] for i in g])
+        if config is not None:
+            b.config = tuple(config)
+            if len(b.config) > 3:
+                b.set_shape(b.config[3])  # before the upload: no extra copy
+        return b
+
+    with cf.ThreadPoolExecutor(1) as ex:
+        fut = ex.submit(plan, groups[0])
+        for ci in range(len(groups)):
+            b = fut.result()
+            if ci + 1 < len(groups):
+                fut = ex.submit(plan, groups[ci + 1])
+            b.allocate(stream=up)  # synchronises `up` only
+            comp.wait_stream(up)
+            b.run(stream=comp)
+            done = torch.cuda.Event()
+            done.record(comp)
+            down.wait_event(done)
+            n = b.output_bytes
+            if ci >= len(host) or host[ci].numel() < n:
+                buf = torch.empty(n, dtype=torch.uint8, pin_memory=True)
+                host[ci:ci + 1] = [buf]
+            lo = int(b.image_off[0])
+            with torch.cuda.stream(down):
+                host[ci][:n].copy_(b.arena[lo: lo + n], non_blocking=True)
+                b.arena.record_stream(down)
+            batches.append(b)
+            h2d += b.upload_bytes
+            d2h += n
+    down.synchronize()
+    for ci, b in enumerate(batches):
+        images.extend(b.host_views(host[ci]))
+        b.close()
+    return images, {"h2d_bytes": h2d, "d2h_bytes": d2h, "groups": len(groups),
+                    "host_buffers": host}
 
 
 def flatten(tiles):

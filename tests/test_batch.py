@@ -124,3 +124,25 @@ def test_autotune_picks_a_config_and_results_do_not_change(cuda, tmp_path, monke
     cfg2, _, table2 = autotune.tune(b)
     assert cfg2 == cfg and table2 is None  # cached
     b.close()
+
+
+@pytest.mark.gpu
+def test_pipelined_host_call_matches_the_batch(cuda):
+    """run_tiles_host (groups planned on a host thread while the previous
+    group runs, images copied down on their own stream) returns, pair by
+    pair, the images one TileBatch run gives."""
+    torch = cuda
+    tiles = small_tiles(7, seed_base=640)
+    kw = tiles[0].setup_kwargs()
+    b = B.TileBatch(tiles, kw).allocate()
+    b.run()
+    torch.cuda.synchronize()
+    ref = [b.image(p).cpu().numpy() for p in range(int(b.info.n_pairs))]
+    b.close()
+    bufs = None
+    for config in ((0, 2, 1, 3), (0, 1, 0, 0)):  # two calls, the second reusing the buffers
+        imgs, st = B.run_tiles_host(tiles, kw, chunks=3, config=config, host_buffers=bufs)
+        bufs = st["host_buffers"]
+        assert st["groups"] == 3 and len(imgs) == len(ref)
+        for a, r in zip(imgs, ref):
+            assert np.array_equal(a, r)
