@@ -555,9 +555,9 @@ __device__ __forceinline__ bool tile_ray(const MarchParams &P, int64_t tile, int
 }
 
 // Vertical ray through its whole column in order (MarchParams::column):
-// labels and axes stream in as 16-byte loads, four voxels at a time (the
-// column starts 16-byte aligned because Z % 4 == 0).  Same arithmetic per
-// step as the warp march.  Interpolation modes need nothing else here: at the
+// labels and axes stream in as 16-byte loads, four voxels at a time, when
+// Z % 4 == 0 (the column then starts 16-byte aligned), else one voxel at a
+// time.  Same arithmetic per step as the warp march, in the same order.  Interpolation modes need nothing else here: at the
 // exact voxel centres of such a ray every interpolation axis collapses.
 __device__ __forceinline__ void march_one_ray_column(const MarchParams &P, int64_t ray,
                                                      const int32_t *__restrict__ label,
@@ -568,55 +568,77 @@ __device__ __forceinline__ void march_one_ray_column(const MarchParams &P, int64
                                                      double *__restrict__ epa_r,
                                                      unsigned long long *__restrict__ counters) {
    const int64_t base = ray * P.Z; // ray = cx * Y + cy: its column (cx, cy, 0..Z-1)
-   const int4 *lab4 = reinterpret_cast<const int4 *>(label + base);
-   const float4 *vec4 = reinterpret_cast<const float4 *>(vec + 3 * base);
    float u1 = 0.f, u2 = 0.f, u3 = -1.f, L = 0.f;
    bool w_zero = false, w_norm = false, bad_label = false;
-   const int nq = (int)(P.Z >> 2);
-   // the next quad's loads are issued before the current quad is processed
-   int q = P.flip_z ? nq - 1 : 0; // mirrored columns are read backwards
-   int4 nl = __ldg(lab4 + q);
-   float4 na = __ldg(vec4 + 3 * q), nb = __ldg(vec4 + 3 * q + 1), nc = __ldg(vec4 + 3 * q + 2);
-   for (int qi = 0; qi < nq; qi++) {
-      const int4 l4 = nl;
-      const float4 a = na, b = nb, c = nc;
-      if (qi + 1 < nq) {
-         q = P.flip_z ? nq - 2 - qi : qi + 1;
-         nl = __ldg(lab4 + q);
-         na = __ldg(vec4 + 3 * q);
-         nb = __ldg(vec4 + 3 * q + 1);
-         nc = __ldg(vec4 + 3 * q + 2);
+   // one voxel of the column, in z order (mirrored for flip_z)
+   auto step = [&](int lab, const F3 &v) {
+      if (lab < 0 || lab >= P.n_props) {
+         bad_label = true;
+         lab = 0;
       }
-      const int labs[4] = {l4.x, l4.y, l4.z, l4.w};
-      const F3 vs[4] = {F3{a.x, a.y, a.z}, F3{a.w, b.x, b.y}, F3{b.z, b.w, c.x},
-                        F3{c.y, c.z, c.w}};
-#pragma unroll
-      for (int jj = 0; jj < 4; jj++) {
-         const int j = P.flip_z ? 3 - jj : jj;
-         int lab = labs[j];
-         if (lab < 0 || lab >= P.n_props) {
-            bad_label = true;
-            lab = 0;
-         }
-         const LabelOptics o = P.lut[lab];
-         if (o.kind == 0)
-            continue;
-         if (o.kind == 1) {
-            L += o.alog;
-            continue;
-         }
-         const F3 v = vs[j];
-         if (is_zero(v)) {
-            w_zero = true;
-            continue;
-         }
-         const float n2 = dot3(v, v);
-         if (n2 - 1.f > 1e-5f)
-            w_norm = true;
-         float cc, ss, cr, sr;
-         if (retard_params(v, n2, o.kret, cc, ss, cr, sr))
-            apply_retard(u1, u2, u3, cc, ss, cr, sr);
+      const LabelOptics o = P.lut[lab];
+      if (o.kind == 0)
+         return;
+      if (o.kind == 1) {
          L += o.alog;
+         return;
+      }
+      if (is_zero(v)) {
+         w_zero = true;
+         return;
+      }
+      const float n2 = dot3(v, v);
+      if (n2 - 1.f > 1e-5f)
+         w_norm = true;
+      float cc, ss, cr, sr;
+      if (retard_params(v, n2, o.kret, cc, ss, cr, sr))
+         apply_retard(u1, u2, u3, cc, ss, cr, sr);
+      L += o.alog;
+   };
+   if ((P.Z & 3) == 0) {
+      // 16-byte columns: labels and axes stream in four voxels at a time;
+      // the next quad's loads are issued before the current quad is processed
+      const int4 *lab4 = reinterpret_cast<const int4 *>(label + base);
+      const float4 *vec4 = reinterpret_cast<const float4 *>(vec + 3 * base);
+      const int nq = (int)(P.Z >> 2);
+      int q = P.flip_z ? nq - 1 : 0; // mirrored columns are read backwards
+      int4 nl = __ldg(lab4 + q);
+      float4 na = __ldg(vec4 + 3 * q), nb = __ldg(vec4 + 3 * q + 1), nc = __ldg(vec4 + 3 * q + 2);
+      for (int qi = 0; qi < nq; qi++) {
+         const int4 l4 = nl;
+         const float4 a = na, b = nb, c = nc;
+         if (qi + 1 < nq) {
+            q = P.flip_z ? nq - 2 - qi : qi + 1;
+            nl = __ldg(lab4 + q);
+            na = __ldg(vec4 + 3 * q);
+            nb = __ldg(vec4 + 3 * q + 1);
+            nc = __ldg(vec4 + 3 * q + 2);
+         }
+         const int labs[4] = {l4.x, l4.y, l4.z, l4.w};
+         const F3 vs[4] = {F3{a.x, a.y, a.z}, F3{a.w, b.x, b.y}, F3{b.z, b.w, c.x},
+                           F3{c.y, c.z, c.w}};
+#pragma unroll
+         for (int jj = 0; jj < 4; jj++) {
+            const int j = P.flip_z ? 3 - jj : jj;
+            step(labs[j], vs[j]);
+         }
+      }
+   } else {
+      // columns of any length: one voxel at a time, the next voxel's loads
+      // issued before the current one is processed
+      const int Z = (int)P.Z, dz = P.flip_z ? -1 : 1;
+      int64_t i = base + (P.flip_z ? Z - 1 : 0);
+      int nlab = __ldg(label + i);
+      F3 nv{__ldg(vec + 3 * i), __ldg(vec + 3 * i + 1), __ldg(vec + 3 * i + 2)};
+      for (int k = 0; k < Z; k++) {
+         const int lab = nlab;
+         const F3 v = nv;
+         if (k + 1 < Z) {
+            i += dz;
+            nlab = __ldg(label + i);
+            nv = F3{__ldg(vec + 3 * i), __ldg(vec + 3 * i + 1), __ldg(vec + 3 * i + 2)};
+         }
+         step(lab, v);
       }
    }
    ray_epilogue(P, ray, u1, u2, L, image, epa_t, epa_d, epa_r, w_zero, w_norm, bad_label,

@@ -273,7 +273,7 @@ int plan_march(const fpgb_setup *s, const int64_t *dim, const double *props, int
    // volume measured; the batched path's autotuner may pick either)
    P.coop = P.mode != 0 ? 1 : 0;
    P.column = 0;
-   if (theta == 0 && P.n_z == P.Z && P.Z % 4 == 0 && step[0] == 0 && step[1] == 0) {
+   if (theta == 0 && P.n_z == P.Z && step[0] == 0 && step[1] == 0) {
       bool seq = true;
       for (int32_t k = 0; k < P.n_z && seq; k++) {
          const ZStep &zs = plan->ztab[k];
@@ -403,7 +403,9 @@ static int prepare_march(const MarchPlan &mp, const int32_t *d_label, const floa
                                  cudaMemcpyHostToDevice, st));
    P.lut = lut;
    P.ztab = zt;
-   if (reinterpret_cast<uintptr_t>(d_label) % 16 || reinterpret_cast<uintptr_t>(d_vec) % 16)
+   // 16-byte column loads (Z % 4 == 0) need 16-byte aligned fields
+   if (P.Z % 4 == 0 &&
+       (reinterpret_cast<uintptr_t>(d_label) % 16 || reinterpret_cast<uintptr_t>(d_vec) % 16))
       P.column = 0;
    return FPGB_OK;
 }

@@ -10,9 +10,10 @@ analysis.  The server thread
   * groups admitted requests into one ``TileBatch`` (batched voxelizer + one
     persistent march over all (tile, tilt) pairs) and launches it on a free
     stream slot, so new batches start while earlier ones still run (the GPU
-    overlaps them).  A batch of a single request goes through the plain
-    per-call kernels instead (no batch planning and upload: lower latency at
-    light load); both paths give the same bits;
+    overlaps them).  While fewer than ``min_batch`` requests wait, they go one
+    at a time through the single-volume kernels instead (no batch planning
+    and upload: lower latency at light and moderate load; two lone requests
+    still overlap on two slots); both paths give the same bits;
   * retires finished batches (CUDA event), copies each request's epa maps to
     the host and completes it.
 
@@ -120,10 +121,16 @@ class GpuRunner:
         import torch
         with torch.cuda.stream(stream):
             b.warnings(stream=stream)  # raises on a label range error
+            # every pair's epa maps gathered on the device, then one copy down
+            blocks = [b.epa_block(p) for p in range(int(b.info.n_pairs))]
+            host = torch.cat([e.reshape(-1) for e in blocks]).cpu().numpy()
+            at = 0
             for t, r in enumerate(reqs):
                 maps = []
-                for p in b.pairs_of(t):  # one copy per pair
-                    e = b.epa_block(p).cpu().numpy()
+                for p in b.pairs_of(t):
+                    n = blocks[p].numel()
+                    e = host[at: at + n].reshape(blocks[p].shape)
+                    at += n
                     maps.append((e[0], e[1], e[2]))
                 images = [b.image(p).clone() for p in b.pairs_of(t)] if self.keep_images else None
                 r.result = {"epa": maps, "images": images}
@@ -134,9 +141,14 @@ class ForwardServer:
     """Continuous batching over ``n_slots`` CUDA streams under an HBM budget."""
 
     def __init__(self, setup, hbm_budget=150e9, max_tiles=32, n_slots=2, runner=None,
-                 streams=None, single_runner=None):
+                 streams=None, single_runner=None, min_batch=4):
         self.budget = float(hbm_budget)
         self.max_tiles = int(max_tiles)
+        # fewer requests than this waiting: launch them one by one on the
+        # single-request path (no batch planning and upload); a TileBatch pays
+        # off once the queue is this long (measured: a batch of 2-3 took
+        # 6.4 ms against 2.6 ms per lone request at 200 requests/s)
+        self.min_batch = int(min_batch)
         self.runner = runner if runner is not None else GpuRunner(setup)
         # batches of one request: the single-volume kernels, the request's
         # tilts overlapped on the library's streams (same results)
@@ -250,7 +262,10 @@ class ForwardServer:
             reqs = []
             if s is not None:
                 with self._lock:
-                    reqs = form_batch(self._pending, self.budget - self._in_bytes, self.max_tiles)
+                    cap = self.max_tiles
+                    if self.single is not None and len(self._pending) < self.min_batch:
+                        cap = 1
+                    reqs = form_batch(self._pending, self.budget - self._in_bytes, cap)
                     for _ in reqs:
                         self._pending.popleft()
             if reqs:

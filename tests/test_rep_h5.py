@@ -149,8 +149,26 @@ def test_simpli_mirror_reproduces_file(cuda):
     assert np.array_equal(np.uint8(res), g["simulation.optic.mask"])
     # this library's own Levenberg-Marquardt: within 1e-3 rad / 1e-3 of MINPACK
     # (the bar of tests/test_rofl.py for noisy pixels)
-    direction, incl, trel, _ = s.apply_rofl(optic_stack(g))
+    stack = optic_stack(g)
+    direction, incl, trel, _ = s.apply_rofl(stack)
     lim = np.rad2deg(1e-3)
-    assert angdist_deg(np.rad2deg(direction), g["analysis.rofl.direction"]).max() < lim
-    assert np.abs(np.rad2deg(incl) - g["analysis.rofl.inclination"]).max() < lim
-    assert np.abs(trel - g["analysis.rofl.trel"]).max() < 1e-3
+    dd = angdist_deg(np.rad2deg(direction), g["analysis.rofl.direction"]).max()
+    di = np.abs(np.rad2deg(incl) - g["analysis.rofl.inclination"]).max()
+    dt = np.abs(trel - g["analysis.rofl.trel"]).max()
+    # the file holds where MINPACK stopped (xtol = ftol = 1.49e-8); this
+    # library's fit converges further: its chi^2 is never above the one of
+    # the file's parameters on the same data (oracle.rofl.fit_residual)
+    from oracle import rofl as R
+    worse = 0.0
+    for i in range(stack.shape[1]):
+        for j in range(stack.shape[2]):
+            ours = R.fit_residual(stack[:, i, j], (direction[i, j], incl[i, j], trel[i, j]))
+            ref = R.fit_residual(stack[:, i, j], (np.deg2rad(g["analysis.rofl.direction"][i, j]),
+                                                  np.deg2rad(g["analysis.rofl.inclination"][i, j]),
+                                                  g["analysis.rofl.trel"][i, j]))
+            worse = max(worse, (ours - ref) / max(ref, 1e-300))
+    import parity
+    parity.record("simpli_rep/rofl_vs_minpack", direction_deg=float(dd), inclination_deg=float(di),
+                  trel_abs=float(dt), chi2_rel_above_minpack=float(worse))
+    assert dd < lim and di < lim and dt < 1e-3
+    assert worse <= 1e-9
