@@ -62,7 +62,7 @@ CPU_SAMPLE_STRIDE = 8      # GPU arm's CPU baseline / parity: every 8th tile (32
 REF_TILES_PER_STEP = 8     # reference arm: 8 consecutive tiles per step, rotating
 VOXELIZER_LAUNCHES = 4     # brick_bin (count), brick_scan, brick_bin (fill), voxel_bricks
 MARCH_LAUNCHES = 2         # batch_march untilted, tilted
-E2E_GROUPS = 4             # host-buffer e2e: tile groups pipelined by run_tiles_host
+E2E_GROUPS = 16            # host-buffer e2e: tile groups pipelined by run_tiles_host (16: 228 ms, 8: 232, 4: 244, 2: 271)
 # units of the committed ncu captures (profiles/*_tiles16.md): the first 16 tiles
 PROFILED_TILTED_STEPS = 268946100   # batch_march, tilted launch
 PROFILED_VOXELS = 67210825          # voxel_bricks
