@@ -8,7 +8,8 @@
   fuses this epilogue (``_Simulator.run_simulation_device(..., epa=True)``).
 * ``rofl(data, ...)`` — ROFL tilt analysis of one pixel's 5-tilt series
   (src/fastpli/analysis/rofl.py:16-63), and ``rofl_device`` for whole maps
-  [5, X, Y, n_rho] (one warp per pixel in ``rofl.cu``).
+  [5, X, Y, n_rho] (one thread per pixel in ``rofl.cu``, MINPACK's
+  Levenberg-Marquardt as the reference's scipy.optimize.leastsq runs it).
 * ``fom_hsv_black(direction, inclination, mask)`` — the colour map of ROFL
   results the pipelines return (images.py:22-56,156-186; numpy on the host).
 

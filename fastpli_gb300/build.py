@@ -16,6 +16,9 @@ Flags that matter for parity:
     per-thread or cooperative) then gives the same bits for the same tile.
   * ``optic.cu``: ``-fmad=false`` — the Gaussian filter sums in scipy's
     order with separate roundings.
+  * ``rofl.cu``: ``-fmad=false`` — MINPACK's and numpy's sums and products
+    round separately; the fused forms numpy's matrix product uses are
+    written out.
 """
 
 import concurrent.futures as cf
@@ -42,6 +45,7 @@ PER_FILE = {"capi.cu": ["-Xcompiler", "-fopenmp"],
             "tissue.cu": ["-fmad=false", "-Xcompiler", "-fopenmp"],
             "voxel_bricks.cu": ["-fmad=false"],
             "optic.cu": ["-fmad=false"],
+            "rofl.cu": ["-fmad=false"],
             "raymarch.cu": ["-fmad=false"],
             "batch.cu": ["-fmad=false", "-Xcompiler", "-fopenmp"]}
 

@@ -238,15 +238,17 @@ int fpgb_epa_device(const double *d_image, int64_t n_pix, int64_t n_rho, double 
  * _ROFL_with_jacobi.py, as Simpli.apply_rofl applies it per pixel,
  * __simpli.py:623-705) of a 5-tilt series d_data [5, n_pix, n_rot] (tilts
  * (0,0), (tau,0), (tau,90), (tau,180), (tau,270) degrees; 4 <= n_rot <= 32),
- * FP64, one warp per pixel.  d_out [n_pix, 8] receives direction,
- * inclination, t_rel, their standard deviations, chi^2 and the number of
- * model evaluations of this implementation's Levenberg-Marquardt fit (the
- * reference counts MINPACK's).  The fit uses the exact Jacobian of the
- * reference's objective (the reference differentiates it by forward
- * differences); grad_mode selects the reference's approximate Jacobian.  Pixels with
- * d_mask[p] == 0 (d_mask may be null) get NaN.  When n_unconverged is
- * non-null the call synchronises and stores the number of pixels that hit
- * the evaluation limit. */
+ * FP64, one thread per pixel.  d_out [n_pix, 8] receives direction,
+ * inclination, t_rel, their standard deviations, chi^2 and MINPACK's
+ * evaluation count (the reference's niter).  The fit is MINPACK's
+ * Levenberg-Marquardt as scipy.optimize.leastsq runs it for the reference
+ * (_ROFL_with_jacobi.py:472-486): forward differences, or with grad_mode
+ * the reference's own Jacobian (lmder); ftol = xtol = 1.49012e-8, at most
+ * 150 evaluations.  Pixels with d_mask[p] == 0 (d_mask may be null) get
+ * NaN.  When n_unconverged is non-null the call synchronises and stores
+ * the number of pixels that stopped at the evaluation limit (MINPACK's
+ * info 5), which the reference passes on silently.
+ */
 int fpgb_rofl_device(const double *d_data, int64_t n_pix, int64_t n_rot, double tilt_angle,
                      double gain, double dir_offset, int grad_mode,
                      const unsigned char *d_mask, double *d_out, int64_t *n_unconverged,

@@ -4,21 +4,26 @@ CPU: the oracle (oracle/rofl.py, scipy's MINPACK as the reference calls it)
 is pinned bit for bit to the reference's own ROFL code on the golden pixels
 (tests/golden/rofl.npz, made by tests/golden/make_rofl_golden.py), and
 reproduces the known answer of tests/analysis/rofl_test.py.
-GPU (rofl.cu, one warp per pixel, FP64, its own Levenberg-Marquardt on the
-same objective with its exact Jacobian):
+GPU (rofl.cu, one thread per pixel, FP64, MINPACK's lmdif / lmder restated
+with the reference's tolerances, scaling and evaluation budget):
   * the rofl_test voxel: direction 0/180 deg within 1e-10, inclination
     +-45 deg within 1e-9, t_rel within 1e-8 of the analytic value (the
     reference test's own bounds);
   * noise-free pixels: the true parameters within 1e-12, the reference within
     1e-10;
-  * noisy pixels: chi^2 no worse than the reference's by more than 1e-12
-    relative (the fit converges at least as far), parameters within 1e-3 of
-    the reference (MINPACK's xtol/ftol stop leaves it up to ~5e-4 away from
-    the minimum along flat directions), standard deviations within 1e-2.
-grad_mode=True uses the reference's approximate Jacobian (derivatives with
-respect to each tilt's own angles, not the fit parameters); where that
-iteration ends depends on the optimizer's path, so only finiteness is tested
-for it."""
+  * noisy pixels, forward differences (grad_mode=False): parameters within
+    1e-5 of the reference, chi^2 within 1e-9 relative, standard deviations
+    within 1e-4 relative, the same evaluation count on at least 95% of the
+    pixels.  The forward-difference Jacobian divides last-bit differences
+    between CUDA's and numpy's FP64 trigonometry by h ~ 1.5e-8, so the
+    iterates part at the 1e-8 level and MINPACK's stopping tests
+    (xtol = ftol = 1.49e-8) may end one step apart; measured on GB300:
+    2.3e-6, 7.6e-11, 8.9e-6, 1 pixel of 192;
+  * grad_mode=True (the reference's own Jacobian, lmder): no finite
+    differences, so the fit follows the reference's to rounding: parameters
+    within 1e-12, chi^2 and deviations within 1e-11 relative on the noisy
+    sets, the same evaluation count on every pixel.
+"""
 
 import os
 import warnings
@@ -102,24 +107,40 @@ def test_device_noise_free_pixels(cuda, name):
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", ["noisy6", "noisy9"])
 def test_device_noisy_pixels(cuda, name):
+    import parity
     g = gold()
     out = _device(cuda, g[name + "|in"])
     ref = g[name + "|grad0|out"]
-    assert np.all(out[:, 6] <= ref[:, 6] * (1 + 1e-12))
-    assert angdist(out[:, 0], ref[:, 0], np.pi).max() < 1e-3
-    assert np.abs(out[:, 1] - ref[:, 1]).max() < 1e-3
-    assert np.abs(out[:, 2] - ref[:, 2]).max() < 1e-3
-    rel = np.abs(out[:, 3:6] - ref[:, 3:6]) / np.abs(ref[:, 3:6])
-    assert rel.max() < 1e-2
-    assert np.all(out[:, 7] > 0)
+    dev = max(angdist(out[:, 0], ref[:, 0], np.pi).max(), np.abs(out[:, 1] - ref[:, 1]).max(),
+              np.abs(out[:, 2] - ref[:, 2]).max())
+    chi = (np.abs(out[:, 6] - ref[:, 6]) / ref[:, 6]).max()
+    std = (np.abs(out[:, 3:6] - ref[:, 3:6]) / np.abs(ref[:, 3:6])).max()
+    same_nfev = float(np.mean(out[:, 7] == ref[:, 7]))
+    parity.record(f"rofl/{name}/lmdif", param_abs=float(dev), chi2_rel=float(chi),
+                  std_rel=float(std), nfev_equal_frac=same_nfev)
+    assert dev < 1e-5
+    assert chi < 1e-9
+    assert std < 1e-4
+    assert same_nfev >= 0.95
 
 
 @pytest.mark.gpu
-def test_device_grad_mode_runs(cuda):
+@pytest.mark.parametrize("name", ["clean6", "noisy6", "clean9", "noisy9"])
+def test_device_grad_mode_matches_reference(cuda, name):
+    import parity
     g = gold()
-    out = _device(cuda, g["noisy9|in"], grad=True)
-    assert np.all(np.isfinite(out))
-    assert np.all((out[:, 0] >= 0) & (out[:, 0] < np.pi))
+    out = _device(cuda, g[name + "|in"], grad=True)
+    ref = g[name + "|grad1|out"]
+    dev = max(angdist(out[:, 0], ref[:, 0], np.pi).max(), np.abs(out[:, 1] - ref[:, 1]).max(),
+              np.abs(out[:, 2] - ref[:, 2]).max())
+    assert np.array_equal(out[:, 7], ref[:, 7])
+    assert dev < 1e-12
+    if name.startswith("noisy"):  # noise-free chi^2 and deviations are rounding noise
+        chi = (np.abs(out[:, 6] - ref[:, 6]) / ref[:, 6]).max()
+        std = (np.abs(out[:, 3:6] - ref[:, 3:6]) / np.abs(ref[:, 3:6])).max()
+        parity.record(f"rofl/{name}/lmder", param_abs=float(dev), chi2_rel=float(chi),
+                      std_rel=float(std))
+        assert chi < 1e-11 and std < 1e-11
 
 
 @pytest.mark.gpu
