@@ -675,9 +675,11 @@ def measure_crossing(dev, steps=10, warmup=3):
                 for t, p in w.tilts]
         e2e.append(time.perf_counter() - t_e)
     del imgs
+    rofl = measure_rofl(w, label, images, stream)
     hbm, _, _ = _peaks()
     return {"workload": "crossing 512x512x120 @ 0.2 um, 2 x 1000 fibers, 5 tilts x 9 angles, "
                         "Slerp",
+            "rofl": rofl,
             "steps_per_s": n_steps / (ms * 1e-3), "ms_per_step": ms, "voxelize_ms": gen_ms,
             "march_ms": march_ms, "tissue_voxels_per_s": tissue / (gen_ms * 1e-3),
             "march_frac_hbm": 16 * n_steps / (march_ms * 1e-3) / (hbm * 1e9),
@@ -686,6 +688,48 @@ def measure_crossing(dev, steps=10, warmup=3):
                              "h2d_bytes_per_step": len(w.tilts) * X * Y * Z * 16,
                              "d2h_bytes_per_step": X * Y * Z * 16 +
                              len(w.tilts) * X * Y * sim.n_rho * 8}}
+
+
+def measure_rofl(w, label, images, stream, reps=3, cpu_pixels=48):
+    """ROFL (Simpli.apply_rofl's fit) of the crossing volume's 5-tilt image
+    series, every tissue pixel, on the device (MINPACK, one thread per
+    pixel), and the oracle (scipy's MINPACK, as the reference) on a sample
+    of the same pixels on one host core."""
+    import torch
+    from fastpli_gb300 import analysis
+    data = torch.stack(images)                        # [5, X, Y, n_rho]
+    mask = (label > 0).any(dim=2)
+    n_pix = int(mask.sum().item())
+    out = {"workload": f"rofl of the crossing images: {n_pix} tissue pixels x 5 tilts x "
+                       f"{data.shape[-1]} angles"}
+    import warnings
+    warnings.simplefilter("ignore")  # pixels at the evaluation limit (grad_mode)
+    for grad in (False, True):
+        analysis.rofl_device(data, mask=mask, grad_mode=grad)
+        torch.cuda.synchronize()
+        t0, t1 = _events(2)
+        t0.record(stream)
+        for _ in range(reps):
+            res = analysis.rofl_device(data, mask=mask, grad_mode=grad)
+        t1.record(stream)
+        torch.cuda.synchronize()
+        ms = t0.elapsed_time(t1) / reps
+        key = "grad_mode" if grad else "forward_differences"
+        out[key] = {"ms": ms, "pixels_per_s": n_pix / (ms * 1e-3)}
+    # the CPU baseline leg: the oracle on a bounded sample of the same pixels
+    from oracle import rofl as O
+    idx = torch.nonzero(mask).cpu().numpy()
+    pick = idx[np.linspace(0, len(idx) - 1, cpu_pixels).astype(int)]
+    host = data.cpu().numpy()
+    t_c = time.perf_counter()
+    for x, y in pick:
+        O.rofl(host[:, x, y, :])
+    dt = time.perf_counter() - t_c
+    out["cpu_baseline"] = {"value": cpu_pixels / dt, "unit": "pixels/s", "cores": 1,
+                           "kind": "port", "sample": f"{cpu_pixels} of the tissue pixels "
+                           "(oracle.rofl: scipy leastsq, forward differences)"}
+    del res
+    return out
 
 
 def measure_watson(dev, steps=3):
@@ -752,16 +796,16 @@ def serve_sweep(rates, seconds, max_requests, min_requests, local, pool_n=N_TILE
         return np.cumsum(gaps), [(pool[i], synth.TILTS_5 if f else synth.TILTS_5[:1])
                                  for i, f in zip(picks, five)]
 
-    # every server instance is warmed before its timed stream: the largest
-    # tiles of the pool once each, so that its worker's cached device buffers
-    # have grown (growing one synchronises the device)
+    # every server instance is warmed before its timed stream
+    # (ForwardServer.start(warm=...)): the pool's 4 largest tiles with 5 tilts
+    # through each of its paths on each stream slot, so that its worker's
+    # cached device buffers have grown (growing one synchronises the device)
     warm = sorted(pool, key=lambda t: -t.n_voxels)[:4]
 
     def serve(server, arrivals, specs):
         reqs = []
-        with server:
-            for r in [server.submit(t, synth.TILTS_5) for t in warm]:
-                r.wait(600)
+        server.start(warm=warm, warm_tilts=synth.TILTS_5)
+        try:
             t0 = time.perf_counter()
             for a, (tile, tilts) in zip(arrivals, specs):
                 d = t0 + a - time.perf_counter()
@@ -770,6 +814,8 @@ def serve_sweep(rates, seconds, max_requests, min_requests, local, pool_n=N_TILE
                 reqs.append(server.submit(tile, tilts))
             for r in reqs:
                 r.wait(600)
+        finally:
+            server.stop()
         wall = time.perf_counter() - t0
         st = serving.latency_stats(reqs)
         st["throughput_rps"] = len(reqs) / wall

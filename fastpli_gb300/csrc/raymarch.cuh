@@ -53,8 +53,8 @@ struct MarchParams {
    const float *vec;
    double *image, *epa_t, *epa_d, *epa_r;
    int32_t tilted; // x/y advance or the axis rotates
-   int32_t column; // vertical ray reading z = 0..Z-1 (or mirrored) in order,
-                   // Z % 4 == 0: the vectorised column path applies
+   int32_t column; // vertical ray reading z = 0..Z-1 (or mirrored) in order:
+                   // the column path applies (16-byte loads when Z % 4 == 0)
    // Lerp/Slerp rays that are not vertical columns: 1 = warp-cooperative
    // march (steps needing interpolation compacted across the warp), 0 = one
    // thread per ray.  Both give the same bits; the choice is speed only.

@@ -164,6 +164,9 @@ class ForwardServer:
         self._run = False
         self._thread = None
         self._next_id = 0
+        self._warm = ([], None)
+        self._warm_error = None
+        self._warm_done = threading.Event()
         self.completed = []
         self.batches = 0
 
@@ -185,13 +188,25 @@ class ForwardServer:
             self._lock.notify()
         return r
 
-    def start(self):
+    def start(self, warm=None, warm_tilts=None):
+        """Starts the worker.  ``warm``: tiles (the largest requests expected)
+        that the worker runs once through every path on every stream slot
+        before it serves: the device buffers a slot caches between requests
+        then have grown, since growing one synchronises the device and under
+        load would stall the other slot's work.  Returns when the warm-up is
+        done."""
         if self._streams is None:
             import torch
             self._streams = [torch.cuda.Stream() for _ in range(self.n_slots)]
         self._run = True
+        self._warm = (list(warm or []), warm_tilts)
+        self._warm_done = threading.Event()
         self._thread = threading.Thread(target=self._loop, name="fpgb-server", daemon=True)
         self._thread.start()
+        self._warm_done.wait()
+        if self._warm_error is not None:
+            self.stop()
+            raise self._warm_error
         return self
 
     def stop(self, timeout=60.0):
@@ -240,9 +255,39 @@ class ForwardServer:
                 still.append((run, h, reqs, ev, s, nb))
         self._inflight = still
 
+    def _warm_up(self):
+        tiles, tilts = self._warm
+        if not tiles:
+            return
+        tilts = np.asarray(tilts if tilts is not None else [(0.0, 0.0)], np.float64)
+
+        def run(runner, group, s):
+            reqs = [Request(-1, t, tilts, 0) for t in group]
+            h, ev = runner.launch(reqs, s)
+            ev.synchronize()
+            runner.collect(h, reqs, s)
+
+        for s in self._streams:
+            if self.single is not None:
+                for t in tiles:
+                    run(self.single, [t], s)
+            if self.max_tiles > 1:
+                run(self.runner, tiles[:self.max_tiles], s)
+            else:
+                for t in tiles:
+                    run(self.runner, [t], s)
+
     def _loop(self):
+        self._warm_error = None
         try:
-            self._serve()
+            self._warm_up()
+        except Exception as e:  # noqa: BLE001 - raised by start()
+            self._warm_error = e
+        finally:
+            self._warm_done.set()
+        try:
+            if self._warm_error is None:
+                self._serve()
         finally:
             if self._streams and not isinstance(self._streams[0], str):
                 # the library's cached buffers of this worker thread
@@ -353,10 +398,15 @@ class PlainRunner:
         return out, ev
 
     def collect(self, h, reqs, stream):
-        for maps, r in zip(h, reqs):
-            if isinstance(maps, list):
-                epa = [tuple(m.cpu().numpy() for m in tdr) for tdr in maps]
-            else:  # one block of every tilt's maps: one copy
-                a = maps.cpu().numpy()
-                epa = [(a[i, 0], a[i, 1], a[i, 2]) for i in range(a.shape[0])]
-            r.result = {"epa": epa, "images": None}
+        import torch
+        # the copies go on the request's own stream, whose work is complete:
+        # on the legacy default stream they would wait for whatever the
+        # library's blocking streams run for other requests
+        with torch.cuda.stream(stream):
+            for maps, r in zip(h, reqs):
+                if isinstance(maps, list):
+                    epa = [tuple(m.cpu().numpy() for m in tdr) for tdr in maps]
+                else:  # one block of every tilt's maps: one copy
+                    a = maps.cpu().numpy()
+                    epa = [(a[i, 0], a[i, 1], a[i, 2]) for i in range(a.shape[0])]
+                r.result = {"epa": epa, "images": None}

@@ -19,6 +19,10 @@ class FakeEvent:
     def query(self):
         return time.perf_counter() >= self.t
 
+    def synchronize(self):
+        while not self.query():
+            time.sleep(0.001)
+
 
 class FakeRunner:
     """Completes each batch after `delay` s; raises for requests whose tile is
@@ -74,6 +78,42 @@ def test_server_batches_and_completes_all():
     assert sum(len(b) for b in runner.batches) == 20
     assert max(len(b) for b in runner.batches) <= 4
     assert len(runner.batches) < 20  # requests arriving together were batched
+
+
+def test_warm_up_runs_every_path_on_every_slot_before_serving():
+    """start(warm=...) runs the warm tiles through the single-request runner
+    one by one and through the batch runner together, on each stream slot,
+    on the worker thread, and returns only when that is done; a warm-up
+    failure is raised by start()."""
+    class SlotRunner(FakeRunner):
+        def launch(self, reqs, stream):
+            with self.lock:
+                self.batches.append((stream, len(reqs), threading.current_thread().name))
+            return [r.rid for r in reqs], FakeEvent(time.perf_counter() + self.delay)
+
+    batch, single = SlotRunner(0.005), SlotRunner(0.005)
+    srv = serving.ForwardServer({"filter_rotations": np.zeros(9)}, hbm_budget=1e12,
+                                max_tiles=8, n_slots=2, runner=batch, single_runner=single,
+                                streams=["s0", "s1"])
+    srv.start(warm=[tile(), tile(), tile()], warm_tilts=[(0, 0)])
+    try:
+        assert sorted(b[:2] for b in single.batches) == [("s0", 1)] * 3 + [("s1", 1)] * 3
+        assert sorted(b[:2] for b in batch.batches) == [("s0", 3), ("s1", 3)]
+        assert {b[2] for b in single.batches + batch.batches} == {"fpgb-server"}
+        r = srv.submit(tile(), [(0, 0)])
+        assert r.wait(10) is not None
+    finally:
+        srv.stop()
+
+    class Broken(FakeRunner):
+        def launch(self, reqs, stream):
+            raise RuntimeError("injected warm-up failure")
+
+    srv = serving.ForwardServer({"filter_rotations": np.zeros(9)}, hbm_budget=1e12,
+                                runner=Broken(), streams=["s0"], n_slots=1)
+    with pytest.raises(RuntimeError, match="warm-up failure"):
+        srv.start(warm=[tile()])
+    assert not srv._thread.is_alive()
 
 
 def test_single_request_batches_use_the_single_runner():
