@@ -690,15 +690,19 @@ def measure_crossing(dev, steps=10, warmup=3):
                              len(w.tilts) * X * Y * sim.n_rho * 8}}
 
 
-def measure_rofl(w, label, images, stream, reps=3, cpu_pixels=48):
+def measure_rofl(w, label, images, stream, reps=3, cpu_pixels=48, side=None):
     """ROFL (Simpli.apply_rofl's fit) of the crossing volume's 5-tilt image
     series, every tissue pixel, on the device (MINPACK, one thread per
     pixel), and the oracle (scipy's MINPACK, as the reference) on a sample
-    of the same pixels on one host core."""
+    of the same pixels on one host core (cpu_pixels = 0: no CPU leg).
+    ``side``: only the first side x side pixels (a small case for ncu)."""
     import torch
     from fastpli_gb300 import analysis
     data = torch.stack(images)                        # [5, X, Y, n_rho]
     mask = (label > 0).any(dim=2)
+    if side:
+        data = data[:, :side, :side].contiguous()
+        mask = mask[:side, :side].contiguous()
     n_pix = int(mask.sum().item())
     out = {"workload": f"rofl of the crossing images: {n_pix} tissue pixels x 5 tilts x "
                        f"{data.shape[-1]} angles"}
@@ -716,6 +720,8 @@ def measure_rofl(w, label, images, stream, reps=3, cpu_pixels=48):
         ms = t0.elapsed_time(t1) / reps
         key = "grad_mode" if grad else "forward_differences"
         out[key] = {"ms": ms, "pixels_per_s": n_pix / (ms * 1e-3)}
+    if not cpu_pixels:
+        return out
     # the CPU baseline leg: the oracle on a bounded sample of the same pixels
     from oracle import rofl as O
     idx = torch.nonzero(mask).cpu().numpy()
@@ -728,8 +734,42 @@ def measure_rofl(w, label, images, stream, reps=3, cpu_pixels=48):
     out["cpu_baseline"] = {"value": cpu_pixels / dt, "unit": "pixels/s", "cores": 1,
                            "kind": "port", "sample": f"{cpu_pixels} of the tissue pixels "
                            "(oracle.rofl: scipy leastsq, forward differences)"}
-    del res
     return out
+
+
+def run_rofl(args):
+    """``--workload rofl``: ROFL alone on the crossing volume's 5-tilt images
+    (the first ``--rofl-side``^2 pixels), as its own line; the small case the
+    ncu summary of rofl_fit is taken on."""
+    import torch
+    import fastpli_gb300
+    from fastpli_gb300 import synth
+    from fastpli_gb300.simulation import _Generator
+    ws, rank, local = _dist_env()
+    torch.cuda.set_device(local)
+    fastpli_gb300.native_library()
+    w = synth.crossing(seed=2)
+    g = _Generator()
+    g.set_volume(w.dim, w.origin, w.voxel_size)
+    g.set_fiber_bundles(w.bundles, w.layers)
+    sim = _simulator(w)
+    label, vector, props, _ = g.run_generation_device(sync_warnings=False)
+    images = sim.run_tilts_device(w.dim, label, vector, props, w.tilts, sync_warnings=False)
+    stream = torch.cuda.current_stream()
+    with ClockSampler(local) as clocks:
+        res = measure_rofl(w, label, images, stream, reps=max(1, args.steps),
+                           cpu_pixels=0 if args.no_cpu else 48, side=args.rofl_side)
+    if rank == 0:
+        fd = res["forward_differences"]
+        line = {"metric": "ROFL pixels/s (MINPACK fit of 5 tilts x 9 angles per pixel, "
+                          "forward differences)", "value": fd["pixels_per_s"],
+                "unit": "pixels/s", "n_gpus": ws, "steps": args.steps, "warmup": 1,
+                "ms_per_step": fd["ms"], "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": res["workload"]}, "detail": res,
+                "clocks": clocks.summary()}
+        print(json.dumps(line), flush=True)
+    return 0
 
 
 def measure_watson(dev, steps=3):
@@ -902,7 +942,10 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="tiles", choices=["tiles", "crossing", "serve"])
+    ap.add_argument("--workload", default="tiles",
+                    choices=["tiles", "crossing", "serve", "rofl"])
+    ap.add_argument("--rofl-side", type=int, default=0,
+                    help="rofl: fit only the first n x n pixels (0: all)")
     ap.add_argument("--rates", type=float, nargs="+", default=[10, 20, 50, 100, 200, 500],
                     help="serving: Poisson arrival rates (requests/s)")
     ap.add_argument("--serve-seconds", type=float, default=3.0,
@@ -926,6 +969,8 @@ def main():
         return run_crossing(args)
     if args.workload == "serve":
         return run_serve(args)
+    if args.workload == "rofl":
+        return run_rofl(args)
     return run_gpu(args)
 
 

@@ -58,6 +58,16 @@ __device__ __forceinline__ double pymod(double a, double b) {
    return m == 0.0 ? 0.0 : m;
 }
 
+// CUDA's FP64 sin, cos, sincos, atan and asin called out of line: one copy
+// of each in the kernel's code instead of one per call site (the fit is
+// bound by instruction fetch while the threads of a warp are in different
+// phases of their fits)
+__device__ __noinline__ double ol_sin(double x) { return sin(x); }
+__device__ __noinline__ double ol_cos(double x) { return cos(x); }
+__device__ __noinline__ void ol_sincos(double x, double *s, double *c) { sincos(x, s, c); }
+__device__ __noinline__ double ol_atan(double x) { return atan(x); }
+__device__ __noinline__ double ol_asin(double x) { return asin(x); }
+
 // _symmetrize_angles (_ROFL_with_jacobi.py:64-74)
 __device__ __forceinline__ void symmetrize(double &dir, double &incl) {
    const double s = -pymod(floor(dir / M_PI), 2.0) + 0.5; // +-0.5
@@ -83,8 +93,8 @@ struct Tilted {
 __device__ __forceinline__ void tilted(const RoflParams &P, double phi, double alpha,
                                        double trel, Tilted &T) {
    double sp, cp, sa, ca;
-   sincos(phi, &sp, &cp);
-   sincos(alpha, &sa, &ca);
+   ol_sincos(phi, &sp, &cp);
+   ol_sincos(alpha, &sa, &ca);
    const double v0 = ca * cp, v1 = ca * sp, v2 = sa;
    T.phi[0] = phi;
    T.alpha[0] = alpha;
@@ -95,8 +105,8 @@ __device__ __forceinline__ void tilted(const RoflParams &P, double phi, double a
       const double w0 = np_dot3(M, v0, v1, v2);
       const double w1 = np_dot3(M + 3, v0, v1, v2);
       const double w2 = np_dot3(M + 6, v0, v1, v2);
-      T.phi[t + 1] = atan(w1 / w0);
-      T.alpha[t + 1] = asin(w2);
+      T.phi[t + 1] = ol_atan(w1 / w0);
+      T.alpha[t + 1] = ol_asin(w2);
       T.trel[t + 1] = trel / P.cos_tau;
    }
 #pragma unroll
@@ -108,8 +118,11 @@ __device__ __forceinline__ void tilted(const RoflParams &P, double phi, double a
 
 // weighted residuals r[i] = w[i] (model_i - c[i]) (_residuum, :407-410) of
 // the 5 R measurements, i = tilt * R + rotation (the order of the
-// reference's flattened intensity curves, :186-212)
-__device__ __forceinline__ void px_residuals(const RoflParams &P, const double *c,
+// reference's flattened intensity curves, :186-212).  Out of line, like the
+// Jacobian and the trust-region step below: one copy of each large body
+// keeps the kernel's code in the instruction cache while the threads of a
+// warp are in different phases of their fits.
+__device__ __noinline__ void px_residuals(const RoflParams &P, const double *c,
                                              const double *w, double phi, double alpha,
                                              double trel, double *r) {
    Tilted T;
@@ -117,11 +130,11 @@ __device__ __forceinline__ void px_residuals(const RoflParams &P, const double *
    const int R = P.n_rot;
 #pragma unroll
    for (int j = 0; j < 5; j++) {
-      const double ca = cos(T.alpha[j]);
-      const double amp = sin(M_PI / 2.0 * T.trel[j] * (ca * ca));
+      const double ca = ol_cos(T.alpha[j]);
+      const double amp = ol_sin(M_PI / 2.0 * T.trel[j] * (ca * ca));
       const int i0 = j * R;
       for (int k = 0; k < R; k++)
-         r[i0 + k] = w[i0 + k] * (amp * sin(2.0 * (P.rho[k] - T.phi[j])) - c[i0 + k]);
+         r[i0 + k] = w[i0 + k] * (amp * ol_sin(2.0 * (P.rho[k] - T.phi[j])) - c[i0 + k]);
    }
 }
 
@@ -129,7 +142,7 @@ __device__ __forceinline__ void px_residuals(const RoflParams &P, const double *
 // angles (_calc_Jacobi, :215-258), weighted (_weighted_jacobi, :393-403):
 // columns J[0..2][i] at J + col[0..2]; used by grad_mode and by the
 // covariance
-__device__ __forceinline__ void px_jacobi(const RoflParams &P, const double *w, double phi,
+__device__ __noinline__ void px_jacobi(const RoflParams &P, const double *w, double phi,
                                           double alpha, double trel, double *J,
                                           const int col[3]) {
    Tilted T;
@@ -137,15 +150,15 @@ __device__ __forceinline__ void px_jacobi(const RoflParams &P, const double *w, 
    const int R = P.n_rot;
 #pragma unroll
    for (int j = 0; j < 5; j++) {
-      const double ca = cos(T.alpha[j]), sa = sin(T.alpha[j]);
+      const double ca = ol_cos(T.alpha[j]), sa = ol_sin(T.alpha[j]);
       const double arg = M_PI / 2.0 * T.trel[j] * (ca * ca);
-      const double sarg = sin(arg), carg = cos(arg);
+      const double sarg = ol_sin(arg), carg = ol_cos(arg);
       const double dal = -M_PI * T.trel[j] * ca * sa * carg; // times s2
       const double dtr = M_PI / 2.0 * (ca * ca);             // times s2, cos(arg)
       const int i0 = j * R;
       for (int k = 0; k < R; k++) {
          const double d2 = 2.0 * (P.rho[k] - T.phi[j]);
-         const double s2 = sin(d2), c2 = cos(d2);
+         const double s2 = ol_sin(d2), c2 = ol_cos(d2);
          const double wi = w[i0 + k];
          J[col[0] + i0 + k] = -2.0 * c2 * sarg * wi;
          J[col[1] + i0 + k] = dal * s2 * wi;
@@ -189,11 +202,25 @@ template <class Get> __device__ __forceinline__ double np_sum(Get get, int n) {
 
 // sum of squares in MINPACK's enorm order (sequential; every value of these
 // fits lies in enorm's unscaled range or is zero)
-__device__ __forceinline__ double seq_sumsq(const double *r, int n) {
+__device__ __noinline__ double seq_sumsq(const double *r, int n) {
    double s = 0.0;
    for (int i = 0; i < n; i++)
       s = s + r[i] * r[i];
    return s;
+}
+
+// sum over i of a[i] b[i], sequential (qrfac's and qtf's column products)
+__device__ __noinline__ double seq_dot(const double *a, const double *b, int n) {
+   double s = 0.0;
+   for (int i = 0; i < n; i++)
+      s = s + a[i] * b[i];
+   return s;
+}
+
+// b[i] = b[i] - t a[i] (qrfac's Householder update)
+__device__ __noinline__ void seq_axmy(const double *a, double *b, double t, int n) {
+   for (int i = 0; i < n; i++)
+      b[i] = b[i] - t * a[i];
 }
 
 // x^3 rounded once, as numpy's x**3 (pow) gives it: the exact cube as a
@@ -236,7 +263,7 @@ __device__ __forceinline__ double mp_norm3(const double v[3]) {
 // qrsolv: solves (R; D) x = (qtb; 0) in the least-squares sense for the
 // 3 x 3 upper triangular R of a pivoted QR (ipvt) and diagonal D; r's
 // strict lower triangle receives S's, sdiag its diagonal
-__device__ void mp_qrsolv(double r[3][3], const int ipvt[3], const double dg[3],
+__device__ __noinline__ void mp_qrsolv(double r[3][3], const int ipvt[3], const double dg[3],
                           const double qtb[3], double x[3], double sdiag[3]) {
    double wa[3];
    for (int j = 0; j < 3; j++) {
@@ -298,7 +325,7 @@ __device__ void mp_qrsolv(double r[3][3], const int ipvt[3], const double dg[3],
 
 // lmpar: the Levenberg-Marquardt parameter par and step x for trust radius
 // delta (r: R in its upper triangle; its lower triangle is scratch)
-__device__ void mp_lmpar(double r[3][3], const int ipvt[3], const double dg[3],
+__device__ __noinline__ void mp_lmpar(double r[3][3], const int ipvt[3], const double dg[3],
                          const double qtb[3], double delta, double &par, double x[3]) {
    double wa1[3], wa2[3], sdiag[3];
    int nsing = 3;
@@ -415,7 +442,7 @@ __device__ int mp_fit(const RoflParams &P, const double *c, const double *w, int
       if (P.grad_mode) {
          px_jacobi(P, w, x[0], x[1], x[2], J, col);
       } else { // fdjac2
-#pragma unroll
+#pragma unroll 1
          for (int j = 0; j < 3; j++) {
             const double temp = x[j];
             double h = epsfd * fabs(temp);
@@ -468,12 +495,9 @@ __device__ int mp_fit(const RoflParams &P, const double *c, const double *w, int
 #pragma unroll
             for (int k = j + 1; k < 3; k++) {
                double *ak = J + col[k];
-               double sum = 0.0;
-               for (int i = j; i < M; i++)
-                  sum = sum + aj[i] * ak[i];
+               const double sum = seq_dot(aj + j, ak + j, M - j);
                const double temp = sum / aj[j];
-               for (int i = j; i < M; i++)
-                  ak[i] = ak[i] - temp * aj[i];
+               seq_axmy(aj + j, ak + j, temp, M - j);
                if (rdiag[k] != 0.0) {
                   const double t2 = ak[j] / rdiag[k];
                   rdiag[k] = rdiag[k] * sqrt(fmax(0.0, 1.0 - t2 * t2));
@@ -506,9 +530,7 @@ __device__ int mp_fit(const RoflParams &P, const double *c, const double *w, int
       for (int j = 0; j < 3; j++) {
          double *aj = J + col[j];
          if (aj[j] != 0.0) {
-            double sum = 0.0;
-            for (int i = j; i < M; i++)
-               sum = sum + aj[i] * wa4[i];
+            const double sum = seq_dot(aj + j, wa4 + j, M - j);
             const double temp = -sum / aj[j];
             for (int i = j; i < M; i++)
                wa4[i] = wa4[i] + aj[i] * temp;
@@ -631,9 +653,12 @@ __device__ int mp_fit(const RoflParams &P, const double *c, const double *w, int
 
 // One thread per pixel.  MAXR bounds n_rot: the measurement arrays of the
 // pixel (7 x 5 MAXR doubles) live in the thread's local memory, which is
-// interleaved across the threads of a warp and cached in L1.
+// interleaved across the threads of a warp and cached in L1.  Held to 96
+// registers (5 CTAs per SM, some values spilled to L1): on 512 x 512 pixels
+// of 5 x 9 measurements 347 ms, against 361 ms at 128 registers (4 CTAs)
+// and 462 ms at 168 (3 CTAs).
 template <int MAXR>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, 5)
 rofl_fit(const double *__restrict__ data, int64_t n_pix, const unsigned char *__restrict__ mask,
          const RoflParams P, double *__restrict__ out, unsigned long long *__restrict__ status) {
    constexpr int MAXM = 5 * MAXR;
