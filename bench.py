@@ -720,7 +720,7 @@ def measure_rofl(w, label, images, stream, reps=3, cpu_pixels=48, side=None):
         ms = t0.elapsed_time(t1) / reps
         key = "grad_mode" if grad else "forward_differences"
         out[key] = {"ms": ms, "pixels_per_s": n_pix / (ms * 1e-3)}
-    if not cpu_pixels:
+    if not cpu_pixels or n_pix == 0:
         return out
     # the CPU baseline leg: the oracle on a bounded sample of the same pixels
     from oracle import rofl as O
