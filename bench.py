@@ -59,6 +59,7 @@ METRIC = "ray-voxel steps/s (uneven tile batch: voxelize + 5 tilts x 9 angles, S
 UNIT = "steps/s"
 N_TILES = 256
 CPU_SAMPLE_STRIDE = 8      # GPU arm's CPU baseline / parity: every 8th tile (32 tiles)
+ONE_THREAD_TILES = (0, 128)  # the CPU baseline's 1-thread figure
 REF_TILES_PER_STEP = 8     # reference arm: 8 consecutive tiles per step, rotating
 VOXELIZER_LAUNCHES = 4     # brick_bin (count), brick_scan, brick_bin (fill), voxel_bricks
 MARCH_LAUNCHES = 2         # batch_march untilted, tilted
@@ -544,10 +545,15 @@ def run_gpu(args):
             threads = os.cpu_count() or 1
             sample = [tiles[t] for t in sample_idx]
             dt, st, outs = cpu_forward(sample, threads, keep=True)
+            one = [tiles[t] for t in ONE_THREAD_TILES]
+            dt1, st1, _ = cpu_forward(one, 1)
             cpu = {"value": st / dt, "unit": UNIT, "cores": threads, "kind": "port",
                    "sample": f"{len(sample)} of the {len(tiles)} tiles (every "
                              f"{CPU_SAMPLE_STRIDE}th), voxelize + 5 tilts each "
-                             "(oracle C restatement, OpenMP)"}
+                             "(oracle C restatement, OpenMP)",
+                   "one_thread": {"value": st1 / dt1, "unit": UNIT, "cores": 1,
+                                  "sample": f"tiles {list(ONE_THREAD_TILES)}, voxelize + 5 "
+                                            "tilts each"}}
             par = parity_of(gpu_sample, outs)
         extra = {}
         if not args.quick:
