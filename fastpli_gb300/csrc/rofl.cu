@@ -664,8 +664,13 @@ rofl_fit(const double *__restrict__ data, int64_t n_pix, const unsigned char *__
    constexpr int MAXM = 5 * MAXR;
    const int R = P.n_rot, M = 5 * R;
    double c[MAXM], w[MAXM], F[2 * MAXM], J[3 * MAXM];
-   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n_pix;
-        p += (int64_t)gridDim.x * blockDim.x) {
+   // pixels are taken one at a time from a counter (status[1]): a thread
+   // whose fit ended early starts the next pixel instead of idling until
+   // the slowest pixel of a fixed share is done
+   for (;;) {
+      const int64_t p = (int64_t)atomicAdd(&status[1], 1ull);
+      if (p >= n_pix)
+         break;
       double *o = out + 8 * p;
       if (mask && !mask[p]) {
 #pragma unroll
@@ -814,10 +819,21 @@ int fpgb_rofl_device(const double *d_data, int64_t n_pix, int64_t n_rot, double 
    void *w = nullptr;
    FPGB_TRY(pool_get(kSlotCounters, sizeof(unsigned long long) * kCounterWords, &w, st));
    auto *status = static_cast<unsigned long long *>(w);
-   FPGB_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(unsigned long long), st));
+   // status[0]: pixels at the evaluation limit, status[1]: next pixel
+   FPGB_CUDA_TRY(cudaMemsetAsync(status, 0, 2 * sizeof(unsigned long long), st));
    if (n_pix > 0) {
-      const int64_t blocks = std::min<int64_t>((n_pix + 127) / 128, 152 * 64);
-      if (P.n_rot <= kRoflSmallRot)
+      // as many CTAs as are resident at once (the pixels are taken from the
+      // counter), fewer for small maps
+      const bool small = P.n_rot <= kRoflSmallRot;
+      int dev = 0, sms = 0, per_sm = 0;
+      FPGB_CUDA_TRY(cudaGetDevice(&dev));
+      FPGB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+      FPGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &per_sm, small ? rofl_fit<kRoflSmallRot> : rofl_fit<kRoflMaxRot>, 128, 0));
+      const int64_t blocks =
+          std::max<int64_t>(1, std::min<int64_t>((n_pix + 127) / 128,
+                                                 (int64_t)sms * std::max(per_sm, 1)));
+      if (small)
          rofl_fit<kRoflSmallRot><<<(unsigned)blocks, 128, 0, st>>>(d_data, n_pix, d_mask, P,
                                                                    d_out, status);
       else
