@@ -81,6 +81,8 @@ struct fpgb_batch_impl {
    int64_t n_untilted = 0; // items [0, n_untilted) untilted, the rest tilted
    int sms = 1;
    int fit[2][2] = {{1, 1}, {1, 1}}; // resident CTAs per SM: [untilted / tilted][per-thread / coop]
+   int fit_columns = 1;               // ... of the columns-only kernel
+   bool untilted_columns = true;      // every untilted pair is a vertical column
    bool narrow = true; // every (tile, tilt) pair allows 32-bit index arithmetic
 };
 
@@ -93,7 +95,11 @@ struct fpgb_batch_impl {
 static_assert(sizeof(MarchParams) % 16 == 0, "MarchParams is copied as int4");
 constexpr int kBatchThreads = 128; // one work item = one CTA-width block of rays
 
-template <int MODE, bool TILT, bool COOP, bool WIDE>
+// COLUMNS: every pair of the launch is a vertical column (MarchParams::column,
+// the untilted pairs of a batch with step 1): the kernel carries only the
+// column path and its few registers (more resident warps for its streaming
+// loads); MODE, TILT, COOP and WIDE are then unused.
+template <int MODE, bool TILT, bool COOP, bool WIDE, bool COLUMNS = false>
 __global__ void __launch_bounds__(128)
 batch_march(const MarchParams *__restrict__ prm, const BatchItem *__restrict__ items,
             int64_t n_items, int chunk, unsigned long long *__restrict__ next,
@@ -102,7 +108,7 @@ batch_march(const MarchParams *__restrict__ prm, const BatchItem *__restrict__ i
    // the item's parameter block, staged in shared memory (read like the
    // plain kernel reads its by-value parameters)
    __shared__ __align__(16) MarchParams sP;
-   __shared__ CoopScratch scratch[COOP ? kBatchThreads / 32 : 1];
+   __shared__ CoopScratch scratch[(COOP && !COLUMNS) ? kBatchThreads / 32 : 1];
    int cur = -1;
    for (;;) {
       if (threadIdx.x == 0)
@@ -136,7 +142,11 @@ batch_march(const MarchParams *__restrict__ prm, const BatchItem *__restrict__ i
             valid = x < sP.X && y < sP.Y;
             ray = valid ? x * sP.Y + y : w.ray_begin;
          }
-         if (!TILT && sP.column) {
+         if constexpr (COLUMNS) {
+            if (valid)
+               march_one_ray_column(sP, ray, sP.label, sP.vec, sP.image, sP.epa_t, sP.epa_d,
+                                    sP.epa_r, counters);
+         } else if (!TILT && sP.column) {
             if (valid)
                march_one_ray_column(sP, ray, sP.label, sP.vec, sP.image, sP.epa_t, sP.epa_d,
                                     sP.epa_r, counters);
@@ -159,6 +169,28 @@ int batch_march_fit_w(int fit[2]) {
        &fit[0], batch_march<MODE, TILT, false, WIDE>, kBatchThreads, 0));
    FPGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
        &fit[1], batch_march<MODE, TILT, true, WIDE>, kBatchThreads, 0));
+   return FPGB_OK;
+}
+
+// resident CTAs per SM of the columns-only kernel
+int batch_columns_fit(int *fit) {
+   FPGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+       fit, batch_march<0, false, false, false, true>, kBatchThreads, 0));
+   return FPGB_OK;
+}
+
+// The untilted pairs when all of them are columns: the columns-only kernel
+// with as many CTAs as are resident.
+int launch_batch_columns(const MarchParams *prm, const BatchItem *items, int64_t n_items,
+                         unsigned long long *next, unsigned long long *counters, int sms,
+                         int fit, int chunk, int shape, cudaStream_t st) {
+   if (n_items <= 0)
+      return FPGB_OK;
+   const int64_t grid = std::min<int64_t>((int64_t)sms * std::max(fit, 1),
+                                          (n_items + chunk - 1) / chunk);
+   batch_march<0, false, false, false, true><<<(unsigned)grid, kBatchThreads, 0, st>>>(
+       prm, items, n_items, chunk, next, counters, shape);
+   FPGB_CUDA_TRY(cudaGetLastError());
    return FPGB_OK;
 }
 
@@ -380,6 +412,8 @@ int plan_batch(int64_t n_tiles, const fpgb_volume *vols, const fpgb_fibers *fibe
          FPGB_TRY(plan_march(&B->setup, dim, P.props.data(), (int64_t)P.props.size() / 2,
                              tilts[2 * k], tilts[2 * k + 1], &mp));
          mp.prm.tilted = (mp.prm.rotate || mp.prm.dx_fx != 0 || mp.prm.dy_fx != 0) ? 1 : 0;
+         if (!mp.prm.tilted && !mp.prm.column)
+            B->untilted_columns = false;
          B->steps += mp.steps;
          B->narrow = B->narrow && march_narrow(mp.prm);
          B->pairs.push_back(std::move(mp));
@@ -520,6 +554,7 @@ int upload_batch(fpgb_batch_impl *B, void *arena, void *ws, cudaStream_t st) {
       FPGB_TRY((batch_march_fit<2, true>(B->fit[1], B->narrow)));
       break;
    }
+   FPGB_TRY(batch_columns_fit(&B->fit_columns));
    return FPGB_OK;
 }
 
@@ -562,9 +597,13 @@ int run_batch(fpgb_batch_impl *B, int march_ctas_per_sm, int chunk, int coop, cu
    const int64_t n0 = B->n_untilted, n1 = (int64_t)B->items.size() - B->n_untilted;
    const int ch = chunk > 0 ? chunk : 4;
 #define FPGB_BATCH_MARCH(M)                                                                    \
-   FPGB_TRY((launch_batch_march<M, false>(prm, items, n0, next, counters, B->sms, B->fit[0],   \
-                                          march_ctas_per_sm, ch, coop, B->narrow, B->shape,     \
-                                          st)));                                               \
+   if (B->untilted_columns)                                                                    \
+      FPGB_TRY(launch_batch_columns(prm, items, n0, next, counters, B->sms, B->fit_columns,    \
+                                    ch, B->shape, st));                                        \
+   else                                                                                        \
+      FPGB_TRY((launch_batch_march<M, false>(prm, items, n0, next, counters, B->sms,           \
+                                             B->fit[0], march_ctas_per_sm, ch, coop,           \
+                                             B->narrow, B->shape, st)));                       \
    FPGB_TRY((launch_batch_march<M, true>(prm, items + n0, n1, next + 1, counters, B->sms,      \
                                          B->fit[1], march_ctas_per_sm, ch, coop, B->narrow,    \
                                          B->shape, st)))
