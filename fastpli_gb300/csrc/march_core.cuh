@@ -624,22 +624,44 @@ __device__ __forceinline__ void march_one_ray_column(const MarchParams &P, int64
          }
       }
    } else {
-      // columns of any length: one voxel at a time, the next voxel's loads
-      // issued before the current one is processed
+      // columns of any length (not 16-byte aligned): four voxels at a time
+      // with scalar loads, the next four's 16 loads issued before the
+      // current four are processed; the last Z % 4 voxels one by one
       const int Z = (int)P.Z, dz = P.flip_z ? -1 : 1;
-      int64_t i = base + (P.flip_z ? Z - 1 : 0);
-      int nlab = __ldg(label + i);
-      F3 nv{__ldg(vec + 3 * i), __ldg(vec + 3 * i + 1), __ldg(vec + 3 * i + 2)};
-      for (int k = 0; k < Z; k++) {
-         const int lab = nlab;
-         const F3 v = nv;
-         if (k + 1 < Z) {
-            i += dz;
-            nlab = __ldg(label + i);
-            nv = F3{__ldg(vec + 3 * i), __ldg(vec + 3 * i + 1), __ldg(vec + 3 * i + 2)};
+      const int n4 = Z >> 2;
+      int64_t i = base + (P.flip_z ? Z - 1 : 0); // next voxel to load, in step order
+      int nl[4];
+      float nx[4], ny[4], nz[4];
+      auto load4 = [&](int64_t i0) {
+#pragma unroll
+         for (int j = 0; j < 4; j++) {
+            const int64_t ij = i0 + j * dz;
+            nl[j] = __ldg(label + ij);
+            nx[j] = __ldg(vec + 3 * ij);
+            ny[j] = __ldg(vec + 3 * ij + 1);
+            nz[j] = __ldg(vec + 3 * ij + 2);
          }
-         step(lab, v);
+      };
+      if (n4 > 0)
+         load4(i);
+      for (int c = 0; c < n4; c++) {
+         int l4[4];
+         F3 v4[4];
+#pragma unroll
+         for (int j = 0; j < 4; j++) {
+            l4[j] = nl[j];
+            v4[j] = F3{nx[j], ny[j], nz[j]};
+         }
+         i += 4 * dz;
+         if (c + 1 < n4)
+            load4(i);
+#pragma unroll
+         for (int j = 0; j < 4; j++)
+            step(l4[j], v4[j]);
       }
+      for (int k = 4 * n4; k < Z; k++, i += dz)
+         step(__ldg(label + i), F3{__ldg(vec + 3 * i), __ldg(vec + 3 * i + 1),
+                                   __ldg(vec + 3 * i + 2)});
    }
    ray_epilogue(P, ray, u1, u2, L, image, epa_t, epa_d, epa_r, w_zero, w_norm, bad_label,
                 counters);
