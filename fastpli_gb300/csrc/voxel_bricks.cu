@@ -105,34 +105,84 @@ __global__ void brick_bin(const SegDev *__restrict__ segs, const int32_t *__rest
    }
 }
 
-// Exclusive scan of the per-brick counts (one CTA; each thread scans a
-// contiguous chunk, the chunk sums are scanned across the block).
+// Exclusive scan of the per-brick counts, one CTA walking the counts in tiles
+// of 1024 x 8: each thread loads 8 consecutive counts (two 16-byte loads when
+// the tile is whole: the arrays start 256-byte aligned and a thread's first
+// index is a multiple of 8), the thread sums are scanned across the block
+// (warp shuffles, then the 32 warp sums) and the running total carries from
+// tile to tile.  offsets[n] receives the total; a total of 2^32 - 1 or more
+// is reported as an overflow of the 32-bit offsets.
+constexpr int kScanPer = 8;
+
 __global__ void __launch_bounds__(1024)
 brick_scan(const unsigned *__restrict__ counts, int64_t n, unsigned *__restrict__ offsets,
            unsigned long long *__restrict__ counters) {
-   __shared__ unsigned long long part[1024];
-   const int t = threadIdx.x;
-   const int64_t per = (n + blockDim.x - 1) / blockDim.x;
-   const int64_t a = n < t * per ? n : t * per, b = n < a + per ? n : a + per;
-   unsigned long long sum = 0;
-   for (int64_t i = a; i < b; i++)
-      sum += counts[i];
-   part[t] = sum;
-   __syncthreads();
-   for (int d = 1; d < (int)blockDim.x; d <<= 1) { // Hillis-Steele inclusive scan
-      const unsigned long long v = t >= d ? part[t - d] : 0ull;
+   __shared__ unsigned long long wsum[32];
+   const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+   // the callers' workspaces are 256-byte aligned; checked anyway before any
+   // 16-byte access
+   const bool vec = (((uintptr_t)counts | (uintptr_t)offsets) & 15) == 0;
+   unsigned long long carry = 0; // total of the tiles before this one (the same in every thread)
+   for (int64_t base = 0; base < n; base += (int64_t)blockDim.x * kScanPer) {
+      const int64_t i0 = base + (int64_t)t * kScanPer;
+      unsigned v[kScanPer];
+      if (vec && i0 + kScanPer <= n) {
+         const uint4 a = *reinterpret_cast<const uint4 *>(counts + i0);
+         const uint4 b = *reinterpret_cast<const uint4 *>(counts + i0 + 4);
+         v[0] = a.x, v[1] = a.y, v[2] = a.z, v[3] = a.w;
+         v[4] = b.x, v[5] = b.y, v[6] = b.z, v[7] = b.w;
+      } else {
+#pragma unroll
+         for (int k = 0; k < kScanPer; k++)
+            v[k] = i0 + k < n ? counts[i0 + k] : 0u;
+      }
+      unsigned long long s = 0;
+#pragma unroll
+      for (int k = 0; k < kScanPer; k++)
+         s += v[k];
+      unsigned long long x = s; // inclusive scan over the warp
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+         const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+         if (lane >= o)
+            x += y;
+      }
+      if (lane == 31)
+         wsum[wid] = x;
       __syncthreads();
-      part[t] += v;
+      if (wid == 0) { // inclusive scan of the warp sums
+         unsigned long long w = lane < (int)(blockDim.x >> 5) ? wsum[lane] : 0ull;
+#pragma unroll
+         for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o)
+               w += y;
+         }
+         wsum[lane] = w;
+      }
       __syncthreads();
+      unsigned long long run = carry + (wid ? wsum[wid - 1] : 0ull) + (x - s);
+      unsigned o8[kScanPer];
+#pragma unroll
+      for (int k = 0; k < kScanPer; k++) {
+         o8[k] = (unsigned)run;
+         run += v[k];
+      }
+      if (vec && i0 + kScanPer <= n) {
+         *reinterpret_cast<uint4 *>(offsets + i0) = make_uint4(o8[0], o8[1], o8[2], o8[3]);
+         *reinterpret_cast<uint4 *>(offsets + i0 + 4) = make_uint4(o8[4], o8[5], o8[6], o8[7]);
+      } else {
+#pragma unroll
+         for (int k = 0; k < kScanPer; k++)
+            if (i0 + k < n)
+               offsets[i0 + k] = o8[k];
+      }
+      carry += wsum[31];
+      __syncthreads(); // wsum is rewritten by the next tile
    }
-   unsigned long long run = part[t] - sum;
-   for (int64_t i = a; i < b; i++) {
-      offsets[i] = (unsigned)run;
-      run += counts[i];
-   }
-   if (t == (int)blockDim.x - 1) {
-      offsets[n] = (unsigned)part[t];
-      if (part[t] >= 0xFFFFFFFFull)
+   if (t == 0) {
+      offsets[n] = (unsigned)carry;
+      if (carry >= 0xFFFFFFFFull)
          atomicOr(&counters[6], (unsigned long long)kStatusOverflow);
    }
 }
