@@ -2,7 +2,7 @@
 
 The persistent march kernel has four knobs that change speed but never
 results: the ray-block shape of its work items (128 consecutive rays, or
-2 x 64, 4 x 32, 8 x 16 rectangles of rays: the footprint of a block's 8-corner
+2 x 64, 4 x 32, 8 x 16, 16 x 8 rectangles of rays: the footprint of a block's 8-corner
 neighbourhoods in a tilted march), the march variant for Lerp/Slerp
 (warp-cooperative with the interpolating steps compacted across the warp, or
 one thread per ray; both give the same bits), work items taken per queue grab,
@@ -27,7 +27,7 @@ _DEFAULT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "aut
 CTAS = (0, 4, 2)        # 0 = as many as fit
 GRABS = (1, 2, 4)
 COOP = (1, 0)
-SHAPES = (0, 1, 2, 3)   # TileBatch.SHAPES
+SHAPES = (0, 1, 2, 3, 4)   # TileBatch.SHAPES
 START = (0, 2, 1, 0)    # (ctas_per_sm, items_per_grab, coop, shape)
 
 
@@ -74,7 +74,7 @@ def key(batch):
     steps_per_ray = batch.steps / max(1, sum(
         int(t.dim[0]) * int(t.dim[1]) * len(batch.pairs_of(i)) for i, t in enumerate(batch.tiles)))
     return (f"{name}|interp{interp}|pairs2^{int(math.log2(max(1, pairs)))}"
-            f"|z2^{int(math.log2(max(1, steps_per_ray)))}|v4")
+            f"|z2^{int(math.log2(max(1, steps_per_ray)))}|v5")
 
 
 def time_config(batch, ctas, grab, coop=1, shape=0, reps=3):

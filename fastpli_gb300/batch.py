@@ -142,7 +142,8 @@ class TileBatch:
                                         self.workspace.data_ptr(), _stream(stream)))
         return self
 
-    SHAPES = ("128 consecutive rays", "2 x 64 rays", "4 x 32 rays", "8 x 16 rays")
+    SHAPES = ("128 consecutive rays", "2 x 64 rays", "4 x 32 rays", "8 x 16 rays",
+              "16 x 8 rays")
 
     def set_shape(self, shape, stream=None):
         """Ray-block shape of the march's work items (``SHAPES``); results do

@@ -72,8 +72,8 @@ int fpgb_batch_run(fpgb_batch *b, int march_ctas_per_sm, int items_per_grab,
                    int march_coop, void *stream);
 /* Ray-block shape of the march's work items (a tuning knob: results are
  * bit-identical across shapes): 0 = blocks of 128 consecutive rays (x * Y + y
- * order, the default), 1, 2, 3 = rectangles of 2 x 64, 4 x 32, 8 x 16 rays
- * (x by y).  Replaces the item list on the device when the batch is bound
+ * order, the default), 1, 2, 3, 4 = rectangles of 2 x 64, 4 x 32, 8 x 16,
+ * 16 x 8 rays (x by y).  Replaces the item list on the device when the batch is bound
  * (synchronises the stream).  A CUDA graph captured before must be captured
  * again. */
 int fpgb_batch_set_shape(fpgb_batch *b, int shape, void *stream);
