@@ -538,6 +538,14 @@ def run_gpu(args):
 
     line = None
     if rank == 0:
+        # the GPU extras first: the CPU legs below load every host core
+        extra = {}
+        if not args.quick:
+            extra["crossing"] = measure_crossing(dev)
+            extra["watson"] = measure_watson(dev)
+            if args.serve_seconds > 0:
+                extra["serving"] = serve_sweep(args.rates, args.serve_seconds,
+                                               args.max_requests, 20, local, pool=tiles)
         cpu, par = None, None
         if ws == 1 and not args.no_cpu:
             import oracle
@@ -555,13 +563,8 @@ def run_gpu(args):
                                   "sample": f"tiles {list(ONE_THREAD_TILES)}, voxelize + 5 "
                                             "tilts each"}}
             par = parity_of(gpu_sample, outs)
-        extra = {}
-        if not args.quick:
-            extra["crossing"] = measure_crossing(dev)
-            extra["watson"] = measure_watson(dev)
-            if args.serve_seconds > 0:
-                extra["serving"] = serve_sweep(args.rates, args.serve_seconds,
-                                               args.max_requests, 20, local, pool=tiles)
+            del outs
+        del gpu_sample
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
