@@ -7,7 +7,6 @@ import warnings
 import numpy as np
 import pytest
 
-import cases
 from fastpli_gb300 import batch as B
 from fastpli_gb300 import synth
 from fastpli_gb300.simulation import _Generator, _Simulator

@@ -10,7 +10,6 @@ before any device work.
 
 Named test_zz_* so that pytest collects it last."""
 
-import ctypes
 import warnings
 
 import numpy as np
