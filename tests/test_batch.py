@@ -104,6 +104,35 @@ def test_batch_bit_identical_to_single_volume_path(cuda, coop, wide, monkeypatch
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("mode,flip_z,step", [("NN", False, 1.0), ("Lerp", True, 1.0),
+                                              ("Slerp", False, 0.7)])
+def test_batch_modes_bit_identical_to_single_volume_path(cuda, mode, flip_z, step):
+    """The other march instantiations of the batch: NN and Lerp, mirrored z,
+    and a step size that makes the untilted rays no columns (the untilted
+    launch then takes the general kernel) all give the single-volume path's
+    bits."""
+    torch = cuda
+    tiles = small_tiles(n=4, seed_base=700)
+    kw = dict(tiles[0].setup_kwargs(), interpolate=mode, flip_z=flip_z, step_size=step)
+    b = B.TileBatch(tiles, kw, epa=True).allocate()
+    b.run()
+    torch.cuda.synchronize()
+    sim = _Simulator()
+    sim.set_pli_setup(kw["step_size"], kw["light_intensity"], kw["voxel_size"], kw["wavelength"],
+                      kw["tissue_refrection"], kw["interpolate"], kw["untilt_sensor_view"],
+                      kw["flip_z"], kw["filter_rotations"])
+    for t, tile in enumerate(tiles):
+        lab, vec = b.label(t).cpu().numpy(), b.vector(t).cpu().numpy()
+        for p in b.pairs_of(t):
+            th, ph = b.tilts[p]
+            with warnings.catch_warnings():
+                warnings.simplefilter("ignore")
+                ref = sim.run_simulation(tile.dim, lab, vec, b.props(t), th, ph)
+            assert np.array_equal(b.image(p).cpu().numpy(), ref), (mode, t, p)
+    b.close()
+
+
+@pytest.mark.gpu
 def test_autotune_picks_a_config_and_results_do_not_change(cuda, tmp_path, monkeypatch):
     torch = cuda
     from fastpli_gb300 import autotune
