@@ -653,12 +653,12 @@ __device__ int mp_fit(const RoflParams &P, const double *c, const double *w, int
 
 // One thread per pixel.  MAXR bounds n_rot: the measurement arrays of the
 // pixel (7 x 5 MAXR doubles) live in the thread's local memory, which is
-// interleaved across the threads of a warp and cached in L1.  Held to 96
-// registers (5 CTAs per SM, some values spilled to L1): on 512 x 512 pixels
-// of 5 x 9 measurements 347 ms, against 361 ms at 128 registers (4 CTAs)
-// and 462 ms at 168 (3 CTAs).
+// interleaved across the threads of a warp and cached in L1.  Held to 80
+// registers (6 CTAs per SM, some values spilled to L1): on 512 x 512 pixels
+// of 5 x 9 measurements 319 ms, against 334 ms at 96 registers (5 CTAs),
+// 361 ms at 128 (4 CTAs) and 462 ms at 168 (3 CTAs).
 template <int MAXR>
-__global__ void __launch_bounds__(128, 5)
+__global__ void __launch_bounds__(128, 6)
 rofl_fit(const double *__restrict__ data, int64_t n_pix, const unsigned char *__restrict__ mask,
          const RoflParams P, double *__restrict__ out, unsigned long long *__restrict__ status) {
    constexpr int MAXM = 5 * MAXR;
